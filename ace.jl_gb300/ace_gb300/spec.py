@@ -1,0 +1,287 @@
+"""Basis specification: 1-particle spec, AA spec, coupling matrix U.
+
+Host-side restatement of ACE.jl's cold construction path, producing the
+index lists every evaluator (GPU kernels and the oracle) consumes:
+
+* 1p spec  -- ``init1pspec!`` (``src/sparsegrids.jl:9-31``): all admissible
+  (mu, n, l, m) in Julia ``CartesianIndices`` order (first symbol fastest),
+  ``m`` forced to -maxL:maxL (``src/product_1pbasis.jl:283-304``), kept when
+  level = (n-1) + l <= maxdeg, then stably sorted by level.
+* AA spec  -- ``gensparse(ordered=true)`` (``src/sparsegrids.jl:55-148``):
+  ascending index tuples of a downset in lexicographic order (so order-major),
+  filtered by the Invariant rule even(sum l) and sum m == 0 for length >= 2
+  (``src/properties.jl:115-125``); rows are then stored reversed
+  (``src/pibasis.jl:90-101``).
+* U        -- ``SymmetricBasis`` (``src/symmbasis.jl:89-162``): one class per
+  AA with all m == 0 (``is_refbasisfcn``, ``src/symmetrygroups.jl:91``),
+  rows from ``rpe_basis``, columns mapped to AA indices through
+  ``_get_ordered`` (A index descending, ``src/symmbasis.jl:174-177``),
+  duplicates summed as ``sparse`` does.
+* cleaning -- ``clean_pibasis!`` / ``clean_1pbasis!``
+  (``src/symmbasis.jl:225-236``, ``src/pibasis.jl:194-207``,
+  ``src/product_1pbasis.jl:345-374``): drop AA columns of U that are zero,
+  then A entries no AA uses, preserving order.
+
+A U entry whose magnitude is below 1e-12 of its row maximum is treated as an
+exact zero before cleaning (the reference keeps round-off-sized columns,
+which depend on its LAPACK).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+import scipy.sparse as sp
+
+from .coupling import _nn_pattern, mrange, rpe_basis
+from .radial import RadialBasis, rn_basis
+
+
+@dataclass
+class OnePSpec:
+    """The A basis: entry i is R_{n_i}(r) Y_{l_i}^{m_i}(rhat) [delta(mu_i, mu_j)]."""
+    mu: np.ndarray       # species index (0-based), all 0 for one species
+    n: np.ndarray        # 1-based radial index
+    l: np.ndarray
+    m: np.ndarray
+
+    def __len__(self):
+        return len(self.n)
+
+    @property
+    def degree(self):
+        return (self.n - 1) + self.l
+
+    def tuples(self):
+        return list(zip(self.mu.tolist(), self.n.tolist(), self.l.tolist(), self.m.tolist()))
+
+
+def init1pspec(nR: int, maxL: int, maxdeg: float, nspecies: int = 1) -> OnePSpec:
+    """init1pspec! for (Categorical?) x Rn x Ylm with SimpleSparseBasis."""
+    mu, n, l, m = [], [], [], []
+    # CartesianIndices over (mu?, n, l, m): first symbol fastest.
+    for mm in range(-maxL, maxL + 1):
+        for ll in range(0, maxL + 1):
+            for nn in range(1, nR + 1):
+                for s in range(nspecies):
+                    if abs(mm) > ll:           # Ylm component admissibility
+                        continue
+                    if (nn - 1) + ll <= maxdeg:  # level1 <= maxlevel1
+                        mu.append(s); n.append(nn); l.append(ll); m.append(mm)
+    mu, n, l, m = map(lambda x: np.array(x, dtype=np.int64), (mu, n, l, m))
+    deg = (n - 1) + l
+    p = np.argsort(deg, kind="stable")     # sort!(spec, by=level): stable
+    return OnePSpec(mu[p], n[p], l[p], m[p])
+
+
+def gensparse_ordered(deg: np.ndarray, ls: np.ndarray, ms: np.ndarray,
+                      maxorder: int, maxdeg: float) -> list:
+    """All ascending tuples v_1 <= ... <= v_k (0-based A indices, k = 0..maxorder)
+    with sum(deg[v]) <= maxdeg, kept when k <= 1 or (sum l even and sum m == 0).
+    Returned per order k as int arrays (N_k, k), each in lexicographic order,
+    which is gensparse's enumeration order (order-major because shorter
+    tuples are padded with leading zeros)."""
+    deg = np.asarray(deg)
+    assert np.all(np.diff(deg) >= 0), "A spec must be sorted by degree"
+    nA = len(deg)
+    out = [np.zeros((1, 0), dtype=np.int64)]  # order 0: the constant
+    for k in range(1, maxorder + 1):
+        # rows: partial tuples, their degree sum and m sum
+        tup = np.zeros((1, 0), dtype=np.int64)
+        dsum = np.zeros(1)
+        msum = np.zeros(1, dtype=np.int64)
+        lsum = np.zeros(1, dtype=np.int64)
+        for t in range(k):
+            rem = k - t
+            lo = tup[:, -1] if t > 0 else np.zeros(len(tup), dtype=np.int64)
+            # remaining rem entries all have degree >= deg[v]
+            hi = np.searchsorted(deg, (maxdeg - dsum) / rem, side="right")
+            cnt = np.maximum(hi - lo, 0)
+            if cnt.sum() == 0:
+                tup = np.zeros((0, t + 1), dtype=np.int64)
+                break
+            rows = np.repeat(np.arange(len(tup)), cnt)
+            starts = np.repeat(lo - np.cumsum(np.concatenate([[0], cnt[:-1]])), cnt)
+            v = np.arange(cnt.sum()) + starts
+            tup = np.concatenate([tup[rows], v[:, None]], axis=1)
+            dsum = dsum[rows] + deg[v]
+            msum = msum[rows] + ms[v]
+            lsum = lsum[rows] + ls[v]
+            keep = dsum <= maxdeg + 1e-12
+            if t < k - 1:
+                # prune: the remaining entries have |m| <= l <= deg <= maxdeg - dsum
+                keep &= np.abs(msum) <= (maxdeg - dsum) + 1e-12
+            tup, dsum, msum, lsum = tup[keep], dsum[keep], msum[keep], lsum[keep]
+        if k >= 2 and len(tup):
+            keep = (lsum % 2 == 0) & (msum == 0)
+            tup = tup[keep]
+        if len(tup):
+            order = np.lexsort(tup.T[::-1])
+            tup = tup[order]
+        out.append(tup)
+    return out
+
+
+@dataclass
+class ACESpec:
+    """Everything an evaluator needs: the radial basis, maxL, the A spec,
+    the AA spec (descending rows, -1 padded), U (CSR nB x nAA) and the
+    per-B degree used for coefficient scaling."""
+    radial: RadialBasis
+    maxL: int
+    nspecies: int
+    aspec: OnePSpec
+    orders: np.ndarray          # (nAA,)
+    iAA2iA: np.ndarray          # (nAA, maxorder), 0-based, -1 padded
+    U: sp.csr_matrix            # (nB, nAA)
+    Bdeg: np.ndarray            # (nB,)
+    Bclass: np.ndarray          # (nB,) index of the class each B row belongs to
+    info: dict = field(default_factory=dict)
+
+    @property
+    def nA(self):
+        return len(self.aspec)
+
+    @property
+    def nAA(self):
+        return len(self.orders)
+
+    @property
+    def nB(self):
+        return self.U.shape[0]
+
+    @property
+    def maxorder(self):
+        return self.iAA2iA.shape[1]
+
+    @property
+    def Leff(self):
+        """Largest l any A entry uses (SH only need to be evaluated to here)."""
+        return int(self.aspec.l.max()) if self.nA else 0
+
+    def ctilde(self, c: np.ndarray) -> np.ndarray:
+        """c~ = U^T c (``_get_eff_coeffs!``, src/evaluator.jl:59-60)."""
+        return np.asarray(self.U.T @ np.asarray(c, dtype=np.float64)).ravel()
+
+
+def _encode(rows: np.ndarray, base: int) -> np.ndarray:
+    """Integer key of each (descending, -1 padded) index row."""
+    k = np.zeros(rows.shape[0], dtype=np.int64)
+    for t in range(rows.shape[1]):
+        k = k * base + (rows[:, t] + 1)
+    return k
+
+
+def symmetric_basis(maxorder: int, maxdeg: float, nR: int | None = None,
+                    maxL: int | None = None, nspecies: int = 1,
+                    r0: float = 1.0, rcut: float = 5.0, rin: float | None = None,
+                    pcut: int = 2, pin: int = 0, p: int = 2,
+                    zero_tol: float = 1e-12) -> ACESpec:
+    """SymmetricBasis(Invariant(), [Categorical *] RnYlm_1pbasis(maxdeg, maxL),
+    SimpleSparseBasis(maxorder, maxdeg)) with cleaning, as ACE.jl builds it."""
+    if nR is None:
+        nR = int(maxdeg)
+    if maxL is None:
+        maxL = int(maxdeg)
+    radial = rn_basis(maxdeg=nR, r0=r0, rcut=rcut, rin=rin, pcut=pcut, pin=pin, p=p)
+
+    aspec = init1pspec(nR, maxL, maxdeg, nspecies)
+    nA0 = len(aspec)
+    deg = aspec.degree.astype(np.float64)
+    per_order = gensparse_ordered(deg, aspec.l, aspec.m, maxorder, maxdeg)
+
+    # PIBasisSpec: reverse rows (descending), pad with -1
+    rows = []
+    orders = []
+    for k, tup in enumerate(per_order):
+        if len(tup) == 0:
+            continue
+        r = -np.ones((len(tup), maxorder), dtype=np.int64)
+        r[:, :k] = tup[:, ::-1]
+        rows.append(r)
+        orders.append(np.full(len(tup), k, dtype=np.int64))
+    iAA2iA = np.concatenate(rows, axis=0)
+    orders = np.concatenate(orders)
+    nAA0 = len(orders)
+    base = nA0 + 1
+    keys = _encode(iAA2iA, base)
+    korder = np.argsort(keys)
+    skeys = keys[korder]
+
+    # dense lookup (mu, n, l, m) -> A index
+    aidx = -np.ones((nspecies, nR + 1, maxL + 1, 2 * maxL + 1), dtype=np.int64)
+    aidx[aspec.mu, aspec.n, aspec.l, aspec.m + maxL] = np.arange(nA0)
+
+    # coupling: loop over reference functions (all m == 0)
+    a_m = aspec.m
+    refmask = np.all(np.where(iAA2iA >= 0, a_m[np.maximum(iAA2iA, 0)] == 0, True), axis=1)
+    Irow, Jcol, vals, Bdeg, Bclass = [], [], [], [], []
+    nB = 0
+    nclass = 0
+    for iAA in np.nonzero(refmask)[0]:
+        k = int(orders[iAA])
+        vs = iAA2iA[iAA, :k]
+        if k == 0:
+            Irow.append(np.array([nB])); Jcol.append(np.array([iAA])); vals.append(np.array([1.0]))
+            Bdeg.append(0.0); Bclass.append(nclass)
+            nB += 1; nclass += 1
+            continue
+        ll = tuple(int(x) for x in aspec.l[vs])
+        nn = tuple((int(a), int(b)) for a, b in zip(aspec.mu[vs], aspec.n[vs]))
+        U = rpe_basis(ll, _nn_pattern(nn))
+        if U.shape[0] == 0:
+            continue
+        mm = mrange(ll)
+        A = np.stack([aidx[aspec.mu[vs[t]], aspec.n[vs[t]], ll[t], mm[:, t] + maxL]
+                      for t in range(k)], axis=1)
+        assert np.all(A >= 0)
+        A = -np.sort(-A, axis=1)                       # _get_ordered
+        r = -np.ones((len(A), maxorder), dtype=np.int64)
+        r[:, :k] = A
+        pk = _encode(r, base)
+        pos = np.searchsorted(skeys, pk)
+        if np.any(pos >= len(skeys)) or np.any(skeys[np.minimum(pos, len(skeys) - 1)] != pk):
+            raise RuntimeError("bcol_ordered not in AA-spec")
+        cols = korder[pos]
+        ucols, inv = np.unique(cols, return_inverse=True)
+        Uc = np.zeros((U.shape[0], len(ucols)))
+        np.add.at(Uc.T, inv, U.T)
+        rmax = np.abs(Uc).max(axis=1, keepdims=True)
+        Uc[np.abs(Uc) <= zero_tol * rmax] = 0.0
+        d = float(sum(aspec.degree[vs]))
+        for irow in range(U.shape[0]):
+            nzm = Uc[irow] != 0
+            Irow.append(np.full(int(nzm.sum()), nB)); Jcol.append(ucols[nzm]); vals.append(Uc[irow, nzm])
+            Bdeg.append(d); Bclass.append(nclass)
+            nB += 1
+        nclass += 1
+    Irow = np.concatenate(Irow); Jcol = np.concatenate(Jcol); vals = np.concatenate(vals)
+    Ufull = sp.csr_matrix((vals, (Irow, Jcol)), shape=(nB, nAA0))
+    Ufull.sum_duplicates()
+
+    # clean_pibasis!: keep non-zero columns (order preserved)
+    colnorm = np.asarray(abs(Ufull).sum(axis=0)).ravel()
+    Inz = np.nonzero(colnorm > 0.0)[0]
+    U = Ufull[:, Inz].tocsr()
+    iAA2iA = iAA2iA[Inz]
+    orders = orders[Inz]
+    # clean_1pbasis!: keep used A entries (order preserved)
+    used = np.zeros(nA0, dtype=bool)
+    used[iAA2iA[iAA2iA >= 0]] = True
+    new_inds = -np.ones(nA0, dtype=np.int64)
+    new_inds[used] = np.arange(used.sum())
+    iAA2iA = np.where(iAA2iA >= 0, new_inds[np.maximum(iAA2iA, 0)], -1)
+    aspec = OnePSpec(aspec.mu[used], aspec.n[used], aspec.l[used], aspec.m[used])
+
+    info = dict(nA_pre=nA0, nAA_pre=nAA0, nclass=nclass,
+                nAA_by_order={int(k): int((orders == k).sum()) for k in np.unique(orders)},
+                maxorder=maxorder, maxdeg=maxdeg, nR=nR, maxL=maxL, nspecies=nspecies)
+    return ACESpec(radial=radial, maxL=maxL, nspecies=nspecies, aspec=aspec,
+                   orders=orders, iAA2iA=iAA2iA, U=U,
+                   Bdeg=np.array(Bdeg), Bclass=np.array(Bclass), info=info)
+
+
+def random_coefficients(spec: ACESpec, seed: int = 0) -> np.ndarray:
+    """c_k ~ N(0,1) / (1 + deg_k)^2, deg_k = sum over the class of (n-1)+l."""
+    rng = np.random.default_rng(seed)
+    return rng.standard_normal(spec.nB) / (1.0 + spec.Bdeg) ** 2
