@@ -1,0 +1,197 @@
+"""ctypes binding of libace_b200 (the C ABI declared in include/ace_b200.h)."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .build import LIB
+
+ACE_OK = 0
+ACE_ERR_INVALID = 1
+ACE_ERR_CUDA = 2
+ACE_ERR_ALLOC = 3
+ACE_ERR_KERNEL = 4
+ACE_ERR_UNSUPPORTED = 5
+
+PREC = {"fp64": 0, "fp32": 1, "fp32_bf16x3": 2}
+
+ACE_INPUTS_ON_DEVICE = 1
+ACE_OUTPUTS_ON_DEVICE = 2
+ACE_ASYNC = 4
+
+EXPORTED = ("ace_ctx_create", "ace_ctx_destroy", "ace_set_params", "ace_set_ctilde",
+            "ace_energy_forces", "ace_energy", "ace_basis", "ace_sync", "ace_get_spec_sizes",
+            "ace_last_error_string", "ace_launch_count")
+
+
+class AceError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"libace_b200 error {code}: {msg}")
+        self.code = code
+
+
+class SpecBundle(C.Structure):
+    _fields_ = [
+        ("version", C.c_int32), ("nR", C.c_int32),
+        ("rA", C.c_void_p), ("rB", C.c_void_p), ("rC", C.c_void_p),
+        ("pl", C.c_int32), ("pr", C.c_int32), ("tl", C.c_double), ("tr", C.c_double),
+        ("tp", C.c_int32), ("r0", C.c_double),
+        ("nA", C.c_int32), ("a_n", C.c_void_p), ("a_l", C.c_void_p), ("a_m", C.c_void_p), ("a_mu", C.c_void_p),
+        ("nspecies", C.c_int32),
+        ("nAA", C.c_int64), ("maxord", C.c_int32), ("orders", C.c_void_p), ("iAA2iA", C.c_void_p),
+        ("nB", C.c_int64), ("U_indptr", C.c_void_p), ("U_indices", C.c_void_p), ("U_data", C.c_void_p),
+    ]
+
+
+_lib = None
+
+
+def load(path: str | None = None):
+    """Load libace_b200.so (it must have been built; the product has no
+    fallback when it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB
+    if not os.path.exists(path):
+        raise RuntimeError(f"libace_b200.so not built at {path}; run __graft_entry__.build()")
+    lib = C.CDLL(path)
+    P = C.c_void_p
+    lib.ace_ctx_create.argtypes = [P, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]
+    lib.ace_ctx_destroy.argtypes = [P]
+    lib.ace_set_params.argtypes = [P, P, C.c_int64]
+    lib.ace_set_ctilde.argtypes = [P, P, C.c_int64]
+    lib.ace_energy_forces.argtypes = [P, C.c_int64, P, P, P, P, P, C.c_int32, P]
+    lib.ace_energy.argtypes = [P, C.c_int64, P, P, P, P, C.c_int32, P]
+    lib.ace_basis.argtypes = [P, C.c_int64, P, P, P, P, P, C.c_int32, P]
+    lib.ace_sync.argtypes = [P]
+    lib.ace_get_spec_sizes.argtypes = [P, P]
+    lib.ace_last_error_string.argtypes = [P]
+    lib.ace_last_error_string.restype = C.c_char_p
+    lib.ace_launch_count.argtypes = [P]
+    lib.ace_launch_count.restype = C.c_int64
+    for name in ("ace_ctx_create", "ace_ctx_destroy", "ace_set_params", "ace_set_ctilde",
+                 "ace_energy_forces", "ace_energy", "ace_basis", "ace_sync", "ace_get_spec_sizes"):
+        getattr(lib, name).restype = C.c_int
+    _lib = lib
+    return lib
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data_as(C.c_void_p)
+    return C.c_void_p(int(a.data_ptr()))  # torch tensor
+
+
+def make_bundle(spec):
+    """SpecBundle (+ the arrays it points to, which must stay alive)."""
+    keep = {}
+    R = spec.radial
+    keep["rA"] = np.ascontiguousarray(R.J.A, dtype=np.float64)
+    keep["rB"] = np.ascontiguousarray(R.J.B, dtype=np.float64)
+    keep["rC"] = np.ascontiguousarray(R.J.C, dtype=np.float64)
+    a = spec.aspec
+    keep["a_n"] = np.ascontiguousarray(a.n - 1, dtype=np.int32)
+    keep["a_l"] = np.ascontiguousarray(a.l, dtype=np.int32)
+    keep["a_m"] = np.ascontiguousarray(a.m, dtype=np.int32)
+    keep["a_mu"] = np.ascontiguousarray(a.mu, dtype=np.int32)
+    keep["orders"] = np.ascontiguousarray(spec.orders, dtype=np.int32)
+    keep["iAA2iA"] = np.ascontiguousarray(spec.iAA2iA, dtype=np.int32)
+    U = spec.U.tocsr()
+    U.sort_indices()
+    keep["U_indptr"] = np.ascontiguousarray(U.indptr, dtype=np.int64)
+    keep["U_indices"] = np.ascontiguousarray(U.indices, dtype=np.int32)
+    keep["U_data"] = np.ascontiguousarray(U.data, dtype=np.float64)
+    b = SpecBundle()
+    b.version = 1
+    b.nR = len(keep["rA"])
+    b.rA, b.rB, b.rC = _ptr(keep["rA"]), _ptr(keep["rB"]), _ptr(keep["rC"])
+    b.pl, b.pr, b.tl, b.tr = R.J.pl, R.J.pr, R.J.tl, R.J.tr
+    b.tp, b.r0 = R.trans.p, R.trans.r0
+    b.nA = spec.nA
+    b.a_n, b.a_l, b.a_m = _ptr(keep["a_n"]), _ptr(keep["a_l"]), _ptr(keep["a_m"])
+    b.a_mu = _ptr(keep["a_mu"])
+    b.nspecies = spec.nspecies
+    b.nAA, b.maxord = spec.nAA, spec.maxorder
+    b.orders, b.iAA2iA = _ptr(keep["orders"]), _ptr(keep["iAA2iA"])
+    b.nB = spec.nB
+    b.U_indptr, b.U_indices, b.U_data = _ptr(keep["U_indptr"]), _ptr(keep["U_indices"]), _ptr(keep["U_data"])
+    return b, keep
+
+
+class Context:
+    """One libace_b200 context: the spec on one device, in one precision."""
+
+    def __init__(self, spec, precision: str = "fp64", device: int = 0):
+        self.lib = load()
+        self.spec = spec
+        self.precision = precision
+        bundle, self._keep = make_bundle(spec)
+        h = C.c_void_p()
+        rc = self.lib.ace_ctx_create(C.byref(bundle), PREC[precision], device, C.byref(h))
+        if rc != ACE_OK:
+            raise AceError(rc, self.lib.ace_last_error_string(None).decode())
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ace_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != ACE_OK:
+            raise AceError(rc, self.lib.ace_last_error_string(self.h).decode())
+
+    def set_params(self, c):
+        c = np.ascontiguousarray(c, dtype=np.float64)
+        self._check(self.lib.ace_set_params(self.h, _ptr(c), len(c)))
+
+    def set_ctilde(self, ct):
+        ct = np.ascontiguousarray(ct, dtype=np.float64)
+        self._check(self.lib.ace_set_ctilde(self.h, _ptr(ct), len(ct)))
+
+    def launch_count(self) -> int:
+        return int(self.lib.ace_launch_count(self.h))
+
+    # host-buffer entry points (numpy in, numpy out)
+    def energy_forces(self, offsets, rr, species=None, forces=True):
+        offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+        rr = np.ascontiguousarray(rr, dtype=np.float64).reshape(-1, 3)
+        sp = None if species is None else np.ascontiguousarray(species, dtype=np.int32)
+        nenv = len(offsets) - 1
+        E = np.empty(nenv)
+        G = np.empty_like(rr) if forces else None
+        self._check(self.lib.ace_energy_forces(self.h, nenv, _ptr(offsets), _ptr(rr), _ptr(sp),
+                                               _ptr(E), _ptr(G), 0, None))
+        return (E, G) if forces else E
+
+    def basis(self, offsets, rr, species=None, grad=False):
+        offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+        rr = np.ascontiguousarray(rr, dtype=np.float64).reshape(-1, 3)
+        sp = None if species is None else np.ascontiguousarray(species, dtype=np.int32)
+        nenv = len(offsets) - 1
+        B = np.empty((nenv, self.spec.nB))
+        dB = np.empty((len(rr), self.spec.nB, 3)) if grad else None
+        self._check(self.lib.ace_basis(self.h, nenv, _ptr(offsets), _ptr(rr), _ptr(sp),
+                                       _ptr(B), _ptr(dB), 0, None))
+        return (B, dB) if grad else B
+
+    # device-buffer entry point (torch CUDA tensors in and out)
+    def energy_forces_device(self, offsets, rr, species, E, G, stream=None, sync=True):
+        flags = ACE_INPUTS_ON_DEVICE | ACE_OUTPUTS_ON_DEVICE | (0 if sync else ACE_ASYNC)
+        st = None if stream is None else C.c_void_p(int(stream))
+        self._check(self.lib.ace_energy_forces(self.h, E.numel(), _ptr(offsets), _ptr(rr), _ptr(species),
+                                               _ptr(E), _ptr(G), flags, st))
+
+    def sync(self):
+        self._check(self.lib.ace_sync(self.h))

@@ -1,0 +1,412 @@
+// ace_b200.cu -- libace_b200: C ABI, context management and host-side
+// validation of the GB300 ACE evaluator.  Kernels live in ace_kernels.cuh.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/ace_b200.h"
+#include "ace_ctx.h"
+#include "ace_kernels.cuh"
+
+using namespace ace;
+
+static thread_local std::string g_create_error;
+
+#define ACE_CUDA(call)                                                            \
+  do {                                                                            \
+    cudaError_t _e = (call);                                                      \
+    if (_e != cudaSuccess) {                                                      \
+      return ctx_fail(ctx, ACE_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e)); \
+    }                                                                             \
+  } while (0)
+
+static int ctx_fail(ace_ctx *ctx, int code, const std::string &msg) {
+  if (ctx) ctx->err = msg; else g_create_error = msg;
+  return code;
+}
+
+template <typename T> static int upload(ace_ctx *ctx, T **dst, const T *src, size_t n) {
+  *dst = nullptr;
+  if (n == 0) return ACE_OK;
+  ACE_CUDA(cudaMalloc((void **)dst, n * sizeof(T)));
+  ctx->allocs.push_back(*dst);
+  ACE_CUDA(cudaMemcpy(*dst, src, n * sizeof(T), cudaMemcpyHostToDevice));
+  return ACE_OK;
+}
+
+static void alp_tables(int L, std::vector<double> &A, std::vector<double> &B) {
+  int sz = size_p(L);
+  A.assign(sz, 0.0);
+  B.assign(sz, 0.0);
+  for (int l = 2; l <= L; ++l) {
+    double ls = double(l * l), lm1s = double((l - 1) * (l - 1));
+    for (int m = 0; m <= l - 2; ++m) {
+      double ms = double(m * m);
+      A[idx_p(l, m)] = std::sqrt((4 * ls - 1.0) / (ls - ms));
+      B[idx_p(l, m)] = -std::sqrt((lm1s - ms) / (4 * lm1s - 1.0));
+    }
+  }
+}
+
+static int validate_spec(const ace_spec_bundle *s, std::string &why) {
+  if (!s) { why = "spec is NULL"; return ACE_ERR_INVALID; }
+  if (s->version != ACE_SPEC_VERSION) { why = "spec version mismatch"; return ACE_ERR_INVALID; }
+  if (s->nR < 1 || s->nR > ACE_MAX_NR) { why = "nR out of range [1, 32]"; return ACE_ERR_UNSUPPORTED; }
+  if (!s->rA || !s->rB || !s->rC) { why = "radial coefficients missing"; return ACE_ERR_INVALID; }
+  if (s->tp < 0 || s->tp > 8 || s->pl < 0 || s->pl > 8 || s->pr < 0 || s->pr > 8) {
+    why = "transform/envelope powers out of range"; return ACE_ERR_UNSUPPORTED;
+  }
+  if (s->nA < 1 || s->nA > 65535) { why = "nA out of range [1, 65535]"; return ACE_ERR_UNSUPPORTED; }
+  if (!s->a_n || !s->a_l || !s->a_m) { why = "A spec arrays missing"; return ACE_ERR_INVALID; }
+  if (s->nspecies < 1 || s->nspecies > 255) { why = "nspecies out of range [1, 255]"; return ACE_ERR_UNSUPPORTED; }
+  if (s->nspecies > 1 && !s->a_mu) { why = "a_mu required for more than one species"; return ACE_ERR_INVALID; }
+  for (int i = 0; i < s->nA; ++i) {
+    if (s->a_n[i] < 0 || s->a_n[i] >= s->nR) { why = "a_n out of range"; return ACE_ERR_INVALID; }
+    if (s->a_l[i] < 0 || s->a_l[i] > ACE_MAX_L) { why = "a_l out of range [0, 20]"; return ACE_ERR_UNSUPPORTED; }
+    if (s->a_m[i] < -s->a_l[i] || s->a_m[i] > s->a_l[i]) { why = "|a_m| > a_l"; return ACE_ERR_INVALID; }
+    if (s->a_mu && (s->a_mu[i] < 0 || s->a_mu[i] >= s->nspecies)) { why = "a_mu out of range"; return ACE_ERR_INVALID; }
+  }
+  if (s->nAA < 1 || s->maxord < 1 || s->maxord > ACE_MAX_ORD) { why = "nAA/maxord out of range (maxord <= 8)"; return ACE_ERR_UNSUPPORTED; }
+  if (!s->orders || !s->iAA2iA) { why = "AA spec arrays missing"; return ACE_ERR_INVALID; }
+  for (int64_t k = 0; k < s->nAA; ++k) {
+    int o = s->orders[k];
+    if (o < 0 || o > s->maxord) { why = "orders out of range"; return ACE_ERR_INVALID; }
+    if (o == 0 && k != 0) { why = "only the first AA function may have order 0"; return ACE_ERR_INVALID; }
+    for (int t = 0; t < o; ++t) {
+      int v = s->iAA2iA[k * s->maxord + t];
+      if (v < 0 || v >= s->nA) { why = "iAA2iA entry out of range"; return ACE_ERR_INVALID; }
+    }
+  }
+  if (s->nB < 0) { why = "nB < 0"; return ACE_ERR_INVALID; }
+  if (s->nB > 0) {
+    if (!s->U_indptr || !s->U_indices || !s->U_data) { why = "U arrays missing"; return ACE_ERR_INVALID; }
+    if (s->U_indptr[0] != 0) { why = "U_indptr[0] != 0"; return ACE_ERR_INVALID; }
+    for (int64_t b = 0; b < s->nB; ++b)
+      if (s->U_indptr[b + 1] < s->U_indptr[b]) { why = "U_indptr not monotone"; return ACE_ERR_INVALID; }
+    for (int64_t k = 0; k < s->U_indptr[s->nB]; ++k)
+      if (s->U_indices[k] < 0 || s->U_indices[k] >= s->nAA) { why = "U index out of range"; return ACE_ERR_INVALID; }
+  }
+  return ACE_OK;
+}
+
+extern "C" int ace_ctx_create(const ace_spec_bundle *s, int32_t prec, int32_t device, ace_ctx **out) {
+  if (!out) return ctx_fail(nullptr, ACE_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  std::string why;
+  int rc = validate_spec(s, why);
+  if (rc != ACE_OK) return ctx_fail(nullptr, rc, why);
+  if (prec != ACE_PREC_FP64 && prec != ACE_PREC_FP32 && prec != ACE_PREC_FP32_BF16X3)
+    return ctx_fail(nullptr, ACE_ERR_UNSUPPORTED, "precision mode not supported");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev)
+    return ctx_fail(nullptr, ACE_ERR_CUDA, "no such CUDA device");
+  ace_ctx *ctx = new ace_ctx();
+  ctx->device = device;
+  ctx->prec = prec;
+  ctx->nR = s->nR; ctx->nA = s->nA; ctx->nAA = s->nAA; ctx->nB = s->nB;
+  ctx->maxord = s->maxord; ctx->nspecies = s->nspecies;
+  ctx->pl = s->pl; ctx->pr = s->pr; ctx->tp = s->tp;
+  ctx->tl = s->tl; ctx->tr = s->tr; ctx->r0 = s->r0;
+  int L = 0;
+  for (int i = 0; i < s->nA; ++i) L = std::max(L, s->a_l[i]);
+  ctx->L = L;
+  auto fail = [&](int code) { ace_ctx_destroy(ctx); return code; };
+  if (cudaSetDevice(device) != cudaSuccess) { g_create_error = "cudaSetDevice failed"; return fail(ACE_ERR_CUDA); }
+  cudaDeviceProp prop;
+  cudaGetDeviceProperties(&prop, device);
+  ctx->nsm = prop.multiProcessorCount;
+  ctx->smem_optin = (int)prop.sharedMemPerBlockOptin;
+
+  // coefficient tables: rA rB rC (nR) alpA alpB (szP), in double and float
+  std::vector<double> alpA, alpB;
+  alp_tables(L, alpA, alpB);
+  std::vector<double> tabD;
+  tabD.insert(tabD.end(), s->rA, s->rA + s->nR);
+  tabD.insert(tabD.end(), s->rB, s->rB + s->nR);
+  tabD.insert(tabD.end(), s->rC, s->rC + s->nR);
+  tabD.insert(tabD.end(), alpA.begin(), alpA.end());
+  tabD.insert(tabD.end(), alpB.begin(), alpB.end());
+  std::vector<float> tabF(tabD.begin(), tabD.end());
+  ctx->ntab = (int)tabD.size();
+  // A spec
+  std::vector<int16_t> an(s->nA), aiy(s->nA), amu(s->nA, 0);
+  for (int i = 0; i < s->nA; ++i) {
+    an[i] = (int16_t)s->a_n[i];
+    aiy[i] = (int16_t)idx_y(s->a_l[i], s->a_m[i]);
+    if (s->a_mu) amu[i] = (int16_t)s->a_mu[i];
+  }
+  // AA spec: orders (uint8) and SoA indices idx[t * nAA + k] (uint16)
+  std::vector<uint8_t> ord(s->nAA);
+  std::vector<uint16_t> idx((size_t)s->maxord * s->nAA, 0);
+  for (int64_t k = 0; k < s->nAA; ++k) {
+    ord[k] = (uint8_t)s->orders[k];
+    for (int t = 0; t < s->orders[k]; ++t) idx[(size_t)t * s->nAA + k] = (uint16_t)s->iAA2iA[k * s->maxord + t];
+  }
+  ctx->has_const = (s->orders[0] == 0);
+  if ((rc = upload(ctx, &ctx->d_tabD, tabD.data(), tabD.size())) ||
+      (rc = upload(ctx, &ctx->d_tabF, tabF.data(), tabF.size())) ||
+      (rc = upload(ctx, &ctx->d_an, an.data(), an.size())) ||
+      (rc = upload(ctx, &ctx->d_aiy, aiy.data(), aiy.size())) ||
+      (rc = upload(ctx, &ctx->d_amu, amu.data(), amu.size())) ||
+      (rc = upload(ctx, &ctx->d_ord, ord.data(), ord.size())) ||
+      (rc = upload(ctx, &ctx->d_idx, idx.data(), idx.size()))) {
+    g_create_error = ctx->err;
+    return fail(rc);
+  }
+  // U (host copy for c~ = U^T c; device copy for the basis path)
+  if (s->nB > 0) {
+    int64_t nnz = s->U_indptr[s->nB];
+    ctx->U_indptr.assign(s->U_indptr, s->U_indptr + s->nB + 1);
+    ctx->U_indices.assign(s->U_indices, s->U_indices + nnz);
+    ctx->U_data.assign(s->U_data, s->U_data + nnz);
+    std::vector<float> uf(ctx->U_data.begin(), ctx->U_data.end());
+    if ((rc = upload(ctx, &ctx->d_Uptr, s->U_indptr, s->nB + 1)) ||
+        (rc = upload(ctx, &ctx->d_Uidx, s->U_indices, nnz)) ||
+        (rc = upload(ctx, &ctx->d_UvalD, s->U_data, nnz)) ||
+        (rc = upload(ctx, &ctx->d_UvalF, uf.data(), uf.size()))) {
+      g_create_error = ctx->err;
+      return fail(rc);
+    }
+  }
+  // coefficients (zero) and status word
+  if (cudaMalloc((void **)&ctx->d_ctD, s->nAA * sizeof(double)) != cudaSuccess ||
+      cudaMalloc((void **)&ctx->d_ctF, s->nAA * sizeof(float)) != cudaSuccess ||
+      cudaMalloc((void **)&ctx->d_status, sizeof(int)) != cudaSuccess) {
+    g_create_error = "cudaMalloc failed";
+    return fail(ACE_ERR_ALLOC);
+  }
+  ctx->allocs.push_back(ctx->d_ctD);
+  ctx->allocs.push_back(ctx->d_ctF);
+  ctx->allocs.push_back(ctx->d_status);
+  cudaMemset(ctx->d_ctD, 0, s->nAA * sizeof(double));
+  cudaMemset(ctx->d_ctF, 0, s->nAA * sizeof(float));
+  cudaMemset(ctx->d_status, 0, sizeof(int));
+  ctx->ctilde.assign(s->nAA, 0.0);
+  if (cudaMallocHost((void **)&ctx->h_status, sizeof(int)) != cudaSuccess) {
+    g_create_error = "cudaMallocHost failed";
+    return fail(ACE_ERR_ALLOC);
+  }
+  if (cudaDeviceSynchronize() != cudaSuccess) { g_create_error = "device sync failed"; return fail(ACE_ERR_CUDA); }
+  rc = kernels_prepare(ctx);
+  if (rc != ACE_OK) { g_create_error = ctx->err; return fail(rc); }
+  *out = ctx;
+  return ACE_OK;
+}
+
+extern "C" int ace_ctx_destroy(ace_ctx *ctx) {
+  if (!ctx) return ACE_OK;
+  cudaSetDevice(ctx->device);
+  cudaDeviceSynchronize();
+  for (void *p : ctx->allocs) cudaFree(p);
+  if (ctx->d_stage) cudaFree(ctx->d_stage);
+  if (ctx->d_scratch) cudaFree(ctx->d_scratch);
+  if (ctx->h_status) cudaFreeHost(ctx->h_status);
+  delete ctx;
+  return ACE_OK;
+}
+
+static int push_ctilde(ace_ctx *ctx) {
+  std::vector<float> f(ctx->ctilde.begin(), ctx->ctilde.end());
+  ACE_CUDA(cudaSetDevice(ctx->device));
+  ACE_CUDA(cudaMemcpy(ctx->d_ctD, ctx->ctilde.data(), ctx->nAA * sizeof(double), cudaMemcpyHostToDevice));
+  ACE_CUDA(cudaMemcpy(ctx->d_ctF, f.data(), ctx->nAA * sizeof(float), cudaMemcpyHostToDevice));
+  return ACE_OK;
+}
+
+extern "C" int ace_set_params(ace_ctx *ctx, const double *c, int64_t nB) {
+  if (!ctx || !c) return ctx_fail(ctx, ACE_ERR_INVALID, "NULL argument");
+  if (nB != ctx->nB) return ctx_fail(ctx, ACE_ERR_INVALID, "length of c != nB");
+  // c~ = U^T c (genmul! with the transposed U, src/evaluator.jl:59-60)
+  std::fill(ctx->ctilde.begin(), ctx->ctilde.end(), 0.0);
+  for (int64_t b = 0; b < nB; ++b)
+    for (int64_t k = ctx->U_indptr[b]; k < ctx->U_indptr[b + 1]; ++k)
+      ctx->ctilde[ctx->U_indices[k]] += ctx->U_data[k] * c[b];
+  return push_ctilde(ctx);
+}
+
+extern "C" int ace_set_ctilde(ace_ctx *ctx, const double *ct, int64_t nAA) {
+  if (!ctx || !ct) return ctx_fail(ctx, ACE_ERR_INVALID, "NULL argument");
+  if (nAA != ctx->nAA) return ctx_fail(ctx, ACE_ERR_INVALID, "length of ctilde != nAA");
+  ctx->ctilde.assign(ct, ct + nAA);
+  return push_ctilde(ctx);
+}
+
+// Host-side validation of host inputs (the library never reads outside the
+// CSR extent it is given; device inputs are checked inside the kernels).
+static int validate_inputs(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const double *rr,
+                           const int32_t *sp) {
+  if (nEnv < 0) return ctx_fail(ctx, ACE_ERR_INVALID, "nEnv < 0");
+  if (off[0] != 0) return ctx_fail(ctx, ACE_ERR_INVALID, "offsets[0] != 0");
+  for (int64_t e = 0; e < nEnv; ++e)
+    if (off[e + 1] < off[e]) return ctx_fail(ctx, ACE_ERR_INVALID, "offsets not monotone");
+  int64_t n = off[nEnv];
+  for (int64_t j = 0; j < n; ++j) {
+    double x = rr[3 * j], y = rr[3 * j + 1], z = rr[3 * j + 2];
+    if (!std::isfinite(x) || !std::isfinite(y) || !std::isfinite(z))
+      return ctx_fail(ctx, ACE_ERR_INVALID, "non-finite position");
+    if (x == 0.0 && y == 0.0 && z == 0.0)
+      return ctx_fail(ctx, ACE_ERR_INVALID, "neighbour at the centre (r == 0)");
+  }
+  if (ctx->nspecies > 1) {
+    if (!sp) return ctx_fail(ctx, ACE_ERR_INVALID, "species required for a multi-species spec");
+    for (int64_t j = 0; j < n; ++j)
+      if (sp[j] < 0 || sp[j] >= ctx->nspecies) return ctx_fail(ctx, ACE_ERR_INVALID, "species out of range");
+  }
+  return ACE_OK;
+}
+
+static int ensure_stage(ace_ctx *ctx, size_t bytes) {
+  if (bytes <= ctx->stage_bytes) return ACE_OK;
+  if (ctx->d_stage) { cudaFree(ctx->d_stage); ctx->d_stage = nullptr; ctx->stage_bytes = 0; }
+  size_t want = std::max(bytes, (size_t)(ctx->stage_bytes * 3 / 2));
+  if (cudaMalloc(&ctx->d_stage, want) != cudaSuccess) return ctx_fail(ctx, ACE_ERR_ALLOC, "staging allocation failed");
+  ctx->stage_bytes = want;
+  return ACE_OK;
+}
+
+static size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
+
+static int read_status(ace_ctx *ctx, cudaStream_t st) {
+  ACE_CUDA(cudaMemcpyAsync(ctx->h_status, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
+  ACE_CUDA(cudaStreamSynchronize(st));
+  int s = *ctx->h_status;
+  if (s != 0) {
+    std::string m = "kernel status:";
+    if (s & ACE_STATUS_BAD_OFFSETS) m += " bad offsets;";
+    if (s & ACE_STATUS_BAD_SPECIES) m += " species out of range;";
+    if (s & ACE_STATUS_BAD_POSITION) m += " bad position;";
+    if (s & ACE_STATUS_SCRATCH) m += " scratch too small;";
+    ctx->err = m;
+    cudaMemsetAsync(ctx->d_status, 0, sizeof(int), st);
+    cudaStreamSynchronize(st);
+    return ACE_ERR_KERNEL;
+  }
+  return ACE_OK;
+}
+
+// Shared driver of the evaluation calls: stages host buffers when needed,
+// launches `run`, copies outputs back.
+template <typename Run>
+static int drive(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, const double *rr,
+                 const int32_t *species, int32_t flags, void *stream,
+                 std::vector<std::pair<void *, size_t>> outs_host_bytes, Run run) {
+  if (!ctx) return ACE_ERR_INVALID;
+  if (nEnv < 0 || !offsets || !rr) return ctx_fail(ctx, ACE_ERR_INVALID, "NULL or negative argument");
+  ACE_CUDA(cudaSetDevice(ctx->device));
+  cudaStream_t st = (cudaStream_t)stream;
+  const bool din = flags & ACE_INPUTS_ON_DEVICE;
+  const bool dout = flags & ACE_OUTPUTS_ON_DEVICE;
+  const int64_t *d_off = offsets;
+  const double *d_rr = rr;
+  const int32_t *d_sp = species;
+  int64_t nNbr = -1;
+  if (!din) {
+    int rc = validate_inputs(ctx, nEnv, offsets, rr, species);
+    if (rc) return rc;
+    nNbr = offsets[nEnv];
+  } else if (ctx->nspecies > 1 && !species) {
+    return ctx_fail(ctx, ACE_ERR_INVALID, "species required for a multi-species spec");
+  }
+  // staging: inputs (if host) + outputs (if host)
+  size_t need = 0;
+  size_t o_off = 0, o_rr = 0, o_sp = 0;
+  if (!din) {
+    o_off = need; need += al256((nEnv + 1) * sizeof(int64_t));
+    o_rr = need; need += al256(std::max<int64_t>(nNbr, 1) * 3 * sizeof(double));
+    if (species && ctx->nspecies > 1) { o_sp = need; need += al256(std::max<int64_t>(nNbr, 1) * sizeof(int32_t)); }
+  }
+  std::vector<size_t> o_out(outs_host_bytes.size());
+  if (!dout)
+    for (size_t i = 0; i < outs_host_bytes.size(); ++i) { o_out[i] = need; need += al256(outs_host_bytes[i].second); }
+  int rc = ensure_stage(ctx, need);
+  if (rc) return rc;
+  char *base = (char *)ctx->d_stage;
+  if (!din) {
+    ACE_CUDA(cudaMemcpyAsync(base + o_off, offsets, (nEnv + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+    ACE_CUDA(cudaMemcpyAsync(base + o_rr, rr, nNbr * 3 * sizeof(double), cudaMemcpyHostToDevice, st));
+    d_off = (const int64_t *)(base + o_off);
+    d_rr = (const double *)(base + o_rr);
+    if (species && ctx->nspecies > 1) {
+      ACE_CUDA(cudaMemcpyAsync(base + o_sp, species, nNbr * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+      d_sp = (const int32_t *)(base + o_sp);
+    } else {
+      d_sp = nullptr;
+    }
+  } else if (ctx->nspecies == 1) {
+    d_sp = nullptr;
+  }
+  std::vector<void *> d_outs(outs_host_bytes.size());
+  for (size_t i = 0; i < outs_host_bytes.size(); ++i)
+    d_outs[i] = (dout || !outs_host_bytes[i].first) ? outs_host_bytes[i].first : (void *)(base + o_out[i]);
+  rc = run(d_off, d_rr, d_sp, d_outs, st);
+  if (rc) return rc;
+  if (!dout) {
+    for (size_t i = 0; i < outs_host_bytes.size(); ++i)
+      if (outs_host_bytes[i].first)
+        ACE_CUDA(cudaMemcpyAsync(outs_host_bytes[i].first, d_outs[i], outs_host_bytes[i].second,
+                                 cudaMemcpyDeviceToHost, st));
+  }
+  if (!(flags & ACE_ASYNC) || !din || !dout) return read_status(ctx, st);
+  return ACE_OK;
+}
+
+extern "C" int ace_energy_forces(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, const double *rr,
+                                 const int32_t *species, double *E, double *dEdrr, int32_t flags,
+                                 void *stream) {
+  if (!ctx) return ACE_ERR_INVALID;
+  if (!E) return ctx_fail(ctx, ACE_ERR_INVALID, "E is NULL");
+  int64_t nNbr = (flags & ACE_INPUTS_ON_DEVICE) ? 0 : (offsets ? offsets[nEnv] : 0);
+  if ((flags & ACE_INPUTS_ON_DEVICE) && dEdrr && !(flags & ACE_OUTPUTS_ON_DEVICE))
+    return ctx_fail(ctx, ACE_ERR_INVALID, "host gradient output needs host inputs (the size is unknown)");
+  std::vector<std::pair<void *, size_t>> outs = {{E, nEnv * sizeof(double)},
+                                                 {dEdrr, (size_t)nNbr * 3 * sizeof(double)}};
+  return drive(ctx, nEnv, offsets, rr, species, flags, stream, outs,
+               [&](const int64_t *o, const double *x, const int32_t *s, std::vector<void *> &d, cudaStream_t st) {
+                 return launch_energy_forces(ctx, nEnv, o, x, s, (double *)d[0], (double *)d[1], st);
+               });
+}
+
+extern "C" int ace_energy(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, const double *rr,
+                          const int32_t *species, double *E, int32_t flags, void *stream) {
+  return ace_energy_forces(ctx, nEnv, offsets, rr, species, E, nullptr, flags, stream);
+}
+
+extern "C" int ace_basis(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, const double *rr,
+                         const int32_t *species, double *B, double *dB, int32_t flags, void *stream) {
+  if (!ctx) return ACE_ERR_INVALID;
+  if (!B) return ctx_fail(ctx, ACE_ERR_INVALID, "B is NULL");
+  if (ctx->nB == 0) return ctx_fail(ctx, ACE_ERR_INVALID, "spec has no U");
+  if (dB && (flags & ACE_INPUTS_ON_DEVICE))
+    return ctx_fail(ctx, ACE_ERR_INVALID, "dB needs host inputs (the size is unknown)");
+  int64_t nNbr = (flags & ACE_INPUTS_ON_DEVICE) ? 0 : (offsets ? offsets[nEnv] : 0);
+  std::vector<std::pair<void *, size_t>> outs = {{B, (size_t)nEnv * ctx->nB * sizeof(double)},
+                                                 {dB, (size_t)nNbr * ctx->nB * 3 * sizeof(double)}};
+  return drive(ctx, nEnv, offsets, rr, species, flags, stream, outs,
+               [&](const int64_t *o, const double *x, const int32_t *s, std::vector<void *> &d, cudaStream_t st) {
+                 return launch_basis(ctx, nEnv, o, x, s, (double *)d[0], (double *)d[1], st);
+               });
+}
+
+extern "C" int ace_sync(ace_ctx *ctx) {
+  if (!ctx) return ACE_ERR_INVALID;
+  ACE_CUDA(cudaSetDevice(ctx->device));
+  ACE_CUDA(cudaDeviceSynchronize());
+  return read_status(ctx, 0);
+}
+
+extern "C" int ace_get_spec_sizes(const ace_ctx *ctx, int64_t *sizes) {
+  if (!ctx || !sizes) return ACE_ERR_INVALID;
+  sizes[0] = ctx->nA; sizes[1] = ctx->nAA; sizes[2] = ctx->nB; sizes[3] = ctx->maxord;
+  return ACE_OK;
+}
+
+extern "C" const char *ace_last_error_string(const ace_ctx *ctx) {
+  return ctx ? ctx->err.c_str() : g_create_error.c_str();
+}
+
+extern "C" int64_t ace_launch_count(const ace_ctx *ctx) { return ctx ? ctx->launches : 0; }

@@ -1,0 +1,350 @@
+"""Benchmark: environment evaluations per second (energy + forces) on one GB300.
+
+Workload (the configuration the metric is quoted on): a single-species
+invariant ACE model of correlation order 4, total degree 12 (Ylm L <= 12,
+Rn = orthogonal polynomials in ((1+r0)/(1+r))^2, r0 = 1, cutoff 5.0),
+100,000 environments with U{20..60} neighbours at radii U[0.8, 5.0] and
+isotropic directions, coefficients c_k ~ N(0,1)/(1+deg_k)^2, seeded.
+
+A step evaluates E and dE/drr for all environments.  `value` times the kernel
+with inputs resident in HBM (L2 flushed between steps); `e2e` times the
+C-ABI call with pinned host buffers (host->device copy of positions,
+device->host copy of energies and gradients inside the timed region).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "ace.jl_gb300"))
+
+METRIC = "env-evals/s (E+F) on 1 GB300: chosen form vs plain FP64 path at <=1e-6 rel err"
+UNIT = "env/s"
+WORKLOAD = dict(name="ace-invariant ord4 deg12 L12, 100k envs, J~U{20..60}",
+                maxorder=4, maxdeg=12, maxL=12, nenv=100_000, jlo=20, jhi=60, seed=2024)
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def build_workload(nenv=None):
+    from ace_gb300.configs import random_batch
+    from ace_gb300.spec import random_coefficients, symmetric_basis
+    spec = symmetric_basis(WORKLOAD["maxorder"], WORKLOAD["maxdeg"], maxL=WORKLOAD["maxL"])
+    c = random_coefficients(spec, seed=WORKLOAD["seed"])
+    b = random_batch(nenv or WORKLOAD["nenv"], WORKLOAD["jlo"], WORKLOAD["jhi"], seed=WORKLOAD["seed"])
+    return spec, c, b
+
+
+def flops_per_env(spec, J):
+    """Algorithmic FLOPs of one environment with J neighbours, counted on the
+    reference algorithm (src/evaluator.jl:121-200) with complex*complex = 6,
+    complex*real = 2, FMA = 2: per neighbour the 1p basis, A accumulation and
+    the force contraction; per environment the AA products and adjoint."""
+    nR, L, nA = len(spec.radial.J.A), spec.Leff, spec.nA
+    szP = (L + 1) * (L + 2) // 2
+    nY = (L + 1) ** 2
+    per_nbr = (10 * nR + 4 * szP + 6 * nY + 4 * nA) + (10 * nR + 8 * szP + 30 * nY + 34 * nA)
+    per_env = 0
+    for k, Nk in spec.info["nAA_by_order"].items():
+        if k == 0:
+            continue
+        per_env += Nk * (6 * (k - 1) + 2) + Nk * (18 * max(k - 2, 0) + 6 + 4 * k)
+    return J * per_nbr + per_env
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index),
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return None
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0])); mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks(torch):
+    """FP32 and FP64 CUDA-core peaks measured here with cuBLAS SGEMM (TF32
+    off) and DGEMM, the non-tensor analogue of the bf16 GEMM peak."""
+    torch.backends.cuda.matmul.allow_tf32 = False
+    out = {}
+    for dt, n, key in ((torch.float32, 8192, "fp32_tflops"), (torch.float64, 4096, "fp64_tflops")):
+        a = torch.randn(n, n, dtype=dt, device="cuda")
+        b = torch.randn(n, n, dtype=dt, device="cuda")
+        for _ in range(2):
+            torch.matmul(a, b)
+        torch.cuda.synchronize()
+        best = 1e30
+        for _ in range(5):
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(); torch.matmul(a, b); e.record(); e.synchronize()
+            best = min(best, s.elapsed_time(e) / 1e3)
+        out[key] = 2 * n ** 3 / best / 1e12
+        del a, b
+    torch.cuda.empty_cache()
+    return out
+
+
+def cpu_baseline(spec, c, b, threads=0, target_s=8.0):
+    """The oracle (FP64 CPU restatement of the reference evaluator) on a
+    bounded sample of the same workload, all host threads."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    orc = oracle.Oracle(spec, c)
+    nthreads = threads or os.cpu_count()
+    n = 256
+    while True:
+        off = b.offsets[:n + 1]
+        t0 = time.perf_counter()
+        orc.energy_forces(off, b.rr[:off[-1]], nthreads=nthreads)
+        dt = time.perf_counter() - t0
+        if dt >= target_s or n >= b.nenv:
+            break
+        n = min(b.nenv, int(n * max(2.0, 1.2 * target_s / max(dt, 1e-3))))
+    return {"value": n / dt, "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": f"first {n} environments of the workload, E+F, FP64, {nthreads} threads, {dt:.1f} s"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    spec, c, b = build_workload()
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    orc = oracle.Oracle(spec, c)
+    nthreads = os.cpu_count()
+    # each step: a bounded sample of the workload (a contiguous block of environments)
+    n = 2048
+    off = b.offsets[:n + 1]
+    t0 = time.perf_counter(); orc.energy_forces(off, b.rr[:off[-1]], nthreads=nthreads); dt = time.perf_counter() - t0
+    n = int(min(b.nenv, max(256, n * 6.0 / max(dt, 1e-3))))
+    times = []
+    for step in range(args.warmup + args.steps):
+        e0 = (step * n) % (b.nenv - n + 1)
+        off = b.offsets[e0:e0 + n + 1] - b.offsets[e0]
+        rr = b.rr[b.offsets[e0]:b.offsets[e0 + n]]
+        t0 = time.perf_counter()
+        orc.energy_forces(off, rr, nthreads=nthreads)
+        if step >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    tot = sum(times)
+    value = n * len(times) / tot
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / len(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded)", "config": {"workload": WORKLOAD["name"], "sample_envs_per_step": n},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
+                             "sample": f"{n} environments per step, E+F, FP64 CPU restatement of the "
+                                       f"reference evaluator (Julia is not available), {nthreads} threads"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--nenv", type=int, default=None, help="smaller workload (profiling only)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    import torch.distributed as dist
+    rank, world, local = dist_info()
+    if world > 1:
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    from ace_gb300.build import build
+    if rank == 0:
+        build()
+    if world > 1:
+        dist.barrier()
+    from ace_gb300.lib import Context
+
+    spec, c, b = build_workload(args.nenv)
+    nenv, nnbr = b.nenv, b.nnbr
+    dev = torch.device("cuda", local)
+    off_d = torch.from_numpy(b.offsets).to(dev)
+    rr_d = torch.from_numpy(b.rr).to(dev)
+    E_d = torch.empty(nenv, dtype=torch.float64, device=dev)
+    G_d = torch.empty_like(rr_d)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # 256 MB > L2
+    stream = torch.cuda.current_stream(dev)
+
+    def timed(ctx, steps, warmup):
+        for _ in range(warmup):
+            ctx.energy_forces_device(off_d, rr_d, None, E_d, G_d, stream=stream.cuda_stream, sync=False)
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        l0 = ctx.launch_count()
+        tot = 0.0
+        for _ in range(steps):
+            flush.zero_()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            ctx.energy_forces_device(off_d, rr_d, None, E_d, G_d, stream=stream.cuda_stream, sync=False)
+            e.record(stream)
+            e.synchronize()
+            tot += s.elapsed_time(e) / 1e3
+        ctx.sync()
+        torch.cuda.synchronize()
+        if world > 1:
+            t = torch.tensor([tot], dtype=torch.float64, device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            tot = float(t.item())
+        return tot, ctx.launch_count() - l0
+
+    # plain FP64 path (the comparison form)
+    ctx64 = Context(spec, "fp64", device=local)
+    ctx64.set_params(c)
+    k64 = max(1, min(args.steps, 3))
+    t64, _ = timed(ctx64, k64, min(args.warmup, 1))
+    E64 = E_d.cpu().numpy().copy(); G64 = G_d.cpu().numpy().copy()
+    # the chosen form: FP32
+    ctx = Context(spec, "fp32", device=local)
+    ctx.set_params(c)
+    with Clocks(local) as clk:
+        t32, launches = timed(ctx, args.steps, args.warmup)
+    clocks = clk.summary()
+    E32 = E_d.cpu().numpy(); G32 = G_d.cpu().numpy()
+    value = nenv * args.steps * world / t32
+    ms = 1e3 * t32 / args.steps
+    scale = np.maximum(np.abs(E64), np.sqrt(np.mean(E64 ** 2)))
+    err = {"E_rel_max_vs_fp64": float(np.max(np.abs(E32 - E64) / scale)),
+           "F_rel_max_vs_fp64": float(np.max(np.abs(G32 - G64)) / np.max(np.abs(G64)))}
+
+    # e2e through the C ABI with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        off_h = torch.from_numpy(b.offsets).pin_memory().numpy()
+        rr_h = torch.from_numpy(b.rr).pin_memory().numpy()
+        E_h = torch.empty(nenv, dtype=torch.float64).pin_memory().numpy()
+        G_h = torch.empty((nnbr, 3), dtype=torch.float64).pin_memory().numpy()
+        import ctypes as C
+        from ace_gb300.lib import _ptr
+        lib = ctx.lib
+
+        def call():
+            rc = lib.ace_energy_forces(ctx.h, nenv, _ptr(off_h), _ptr(rr_h), None, _ptr(E_h), _ptr(G_h), 0, None)
+            assert rc == 0, lib.ace_last_error_string(ctx.h)
+        for _ in range(args.warmup):
+            call()
+        if world > 1:
+            dist.barrier()
+        tt = 0.0
+        for _ in range(args.steps):
+            flush.zero_(); torch.cuda.synchronize()
+            t0 = time.perf_counter(); call(); tt += time.perf_counter() - t0
+        if world > 1:
+            t = torch.tensor([tt], dtype=torch.float64, device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            tt = float(t.item())
+        e2e = {"value": nenv * args.steps * world / tt, "unit": UNIT,
+               "h2d_bytes_per_step": int(off_h.nbytes + rr_h.nbytes),
+               "d2h_bytes_per_step": int(E_h.nbytes + G_h.nbytes)}
+
+    if rank != 0:
+        if world > 1:
+            dist.barrier()
+        return
+    peaks = measured_peaks(torch)
+    Jmean = nnbr / nenv
+    fl = flops_per_env(spec, Jmean) * nenv
+    achieved = fl / (t32 / args.steps) / 1e12
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "ef_kernel_fp32_traffic.json")
+    if os.path.exists(tpath):
+        tr = json.load(open(tpath))
+        traffic = tr["dram_bytes_per_env"] * nenv
+    roof = {"bound": "fp32", "achieved": achieved, "peak": peaks["fp32_tflops"], "unit": "TFLOP/s",
+            "frac": achieved / peaks["fp32_tflops"], "traffic": traffic,
+            "kernel": "ef_kernel<float> (fused 1p basis, A, AA, adjoint, forces)",
+            "peak_source": "measured in this run: cuBLAS SGEMM 8192^3, TF32 off (CUDA-core FP32)",
+            "flops_per_env": fl / nenv}
+    cpu = None if args.no_cpu else cpu_baseline(spec, c, b)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOAD["name"], "nenv_per_gpu": nenv, "nnbr_per_gpu": nnbr,
+                       "form": "fp32 (Rn/Ylm/A/AA/adjoint in FP32, energy block sums in FP64)",
+                       "l2": "flushed (256 MB write) between timed steps", "parallelism": f"replicas x{world}"},
+            "forms": {"fp64": {"value": nenv * k64 * world / t64, "ms_per_step": 1e3 * t64 / k64},
+                      "fp32": {"value": value, "ms_per_step": ms}},
+            "error": err, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
+            "gpu_launches": int(launches), "peaks_measured": peaks}
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.barrier()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,148 @@
+/*
+ * ace_b200.h -- C ABI of libace_b200, a GB300 (sm_103a) evaluator for linear
+ * ACE models.  Plain pointers and sizes only; every call returns an int
+ * status (ACE_OK == 0) and no exception crosses the ABI.
+ *
+ * The library replaces the CPU evaluation that ACE.jl performs through Julia
+ * dispatch (the reference has no FFI; the entry points below are what a
+ * Julia `ccall` shim, or any C caller, binds):
+ *
+ *   ace_ctx_create      <- LinearACEModel(basis, c; evaluator=:standard)
+ *                          src/linearmodel.jl:44-56, ProductEvaluator(basis, c)
+ *                          src/evaluator.jl:30-31
+ *   ace_set_params      <- set_params!(m, c)  src/linearmodel.jl:67-71,
+ *                          src/evaluator.jl:48-56 (c~ = U^T c, :59-60)
+ *   ace_energy          <- evaluate(m::LinearACEModel, cfg)
+ *                          src/linearmodel.jl:107-108 -> src/evaluator.jl:121-147
+ *   ace_energy_forces   <- evaluate + grad_config(m, cfg)
+ *                          src/linearmodel.jl:110-111 -> src/evaluator.jl:150-200
+ *   ace_basis           <- evaluate(basis::SymmetricBasis, cfg) and
+ *                          evaluate_d / evaluate_ed   src/symmbasis.jl:297-336
+ *                          (grad_params = B, grad_params_config = dB,
+ *                          src/linearmodel.jl:114-128)
+ *
+ * Many environments are evaluated per call: environment e owns neighbours
+ * offsets[e] .. offsets[e+1]-1 of the position array (CSR).  Positions are
+ * rr_j = X_j - X_centre, stored as x,y,z triples (the memory layout of a
+ * Julia Vector{SVector{3,Float64}}).
+ *
+ * Ownership: the caller owns all input and output buffers; the context owns
+ * every device allocation it makes.  Threading: one context per host thread
+ * (or per stream); calls on one context must not overlap.
+ */
+#ifndef ACE_B200_H
+#define ACE_B200_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ACE_SPEC_VERSION 1
+
+/* status codes */
+enum {
+  ACE_OK = 0,
+  ACE_ERR_INVALID = 1,      /* invalid argument or input data (see ace_last_error_string) */
+  ACE_ERR_CUDA = 2,         /* a CUDA runtime call failed */
+  ACE_ERR_ALLOC = 3,        /* device or host allocation failed */
+  ACE_ERR_KERNEL = 4,       /* a kernel reported a bad status word */
+  ACE_ERR_UNSUPPORTED = 5,  /* the spec exceeds a compiled limit */
+  ACE_ERR_EMPTY_ENV = 6     /* informational: an environment had no neighbours */
+};
+
+/* precision modes */
+enum {
+  ACE_PREC_FP64 = 0,        /* all arithmetic in FP64 */
+  ACE_PREC_FP32 = 1,        /* Rn/Ylm/A/AA in FP32, energy sums in FP64 */
+  ACE_PREC_FP32_BF16X3 = 2, /* FP32, plus split-BF16 (3-pass) tensor-core U*AA for ace_basis */
+  ACE_PREC_LEARNED = 3      /* reserved: learned radial compression */
+};
+
+/* flags for the evaluation calls */
+enum {
+  ACE_INPUTS_ON_DEVICE = 1,   /* offsets/rr/species are device pointers */
+  ACE_OUTPUTS_ON_DEVICE = 2,  /* E/dEdrr/B/dB are device pointers */
+  ACE_ASYNC = 4               /* with device inputs and outputs: do not synchronise */
+};
+
+/*
+ * The basis specification (the product of basis construction; see the
+ * spec builder in the host package).  All arrays are host memory and are
+ * copied by ace_ctx_create.
+ *
+ *   radial:  R_n(r) = P_n(t(r)), t(r) = ((1+r0)/(1+r))^tp,
+ *            P_1 = rA[0] fcut(t), P_2 = (rA[1] t + rB[1]) P_1,
+ *            P_n = (rA[n-1] t + rB[n-1]) P_{n-1} + rC[n-1] P_{n-2},
+ *            fcut(t) = (t-tl)^pl (t-tr)^pr, zero if pl>0 && t<tl or pr>0 && t>tr
+ *   1p:      A_i = sum_j [mu_j == a_mu[i]] R_{a_n[i]}(r_j) Y_{a_l[i]}^{a_m[i]}(rhat_j)
+ *            (a_n 0-based; a_mu may be NULL for one species)
+ *   AA:      AA_k = prod_{t < orders[k]} A_{iAA2iA[k*maxord + t]}  (row-major, -1 padded)
+ *   U:       B = U AA  (CSR, nB x nAA)
+ */
+typedef struct {
+  int32_t version;
+  int32_t nR;
+  const double *rA, *rB, *rC;
+  int32_t pl, pr;
+  double tl, tr;
+  int32_t tp;
+  double r0;
+  int32_t nA;
+  const int32_t *a_n, *a_l, *a_m, *a_mu;
+  int32_t nspecies;
+  int64_t nAA;
+  int32_t maxord;
+  const int32_t *orders;
+  const int32_t *iAA2iA;
+  int64_t nB;
+  const int64_t *U_indptr;
+  const int32_t *U_indices;
+  const double *U_data;
+} ace_spec_bundle;
+
+typedef struct ace_ctx ace_ctx;
+
+/* Create a context on CUDA device `device`: copies the spec to the device
+   and prepares the evaluation tables.  Coefficients start at zero. */
+int ace_ctx_create(const ace_spec_bundle *spec, int32_t precision_mode, int32_t device,
+                   ace_ctx **out);
+int ace_ctx_destroy(ace_ctx *ctx);
+
+/* set_params!: B-basis coefficients c (length nB); c~ = U^T c is formed on the host. */
+int ace_set_params(ace_ctx *ctx, const double *c, int64_t nB);
+/* The AA-basis coefficients c~ directly (length nAA). */
+int ace_set_ctilde(ace_ctx *ctx, const double *ctilde, int64_t nAA);
+
+/* Site energies E[e] and gradients dEdrr[3*j + a] = dE_{e(j)}/d rr_j[a]
+   (grad_config; forces on neighbours are -dEdrr).  dEdrr may be NULL.
+   species may be NULL for a one-species spec.  `stream` is a cudaStream_t
+   (NULL = the legacy default stream). */
+int ace_energy_forces(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, const double *rr,
+                      const int32_t *species, double *E, double *dEdrr, int32_t flags,
+                      void *stream);
+int ace_energy(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, const double *rr,
+               const int32_t *species, double *E, int32_t flags, void *stream);
+
+/* Symmetric basis B[e*nB + b]; if dB != NULL also
+   dB[(j*nB + b)*3 + a] = dB_b(env of j)/d rr_j[a]. */
+int ace_basis(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, const double *rr,
+              const int32_t *species, double *B, double *dB, int32_t flags, void *stream);
+
+/* Wait for the context's outstanding work; returns the kernels' status. */
+int ace_sync(ace_ctx *ctx);
+
+/* sizes[0..3] = nA, nAA, nB, maxord */
+int ace_get_spec_sizes(const ace_ctx *ctx, int64_t *sizes);
+
+/* Last error message of this context (or of the last failed create when ctx is NULL). */
+const char *ace_last_error_string(const ace_ctx *ctx);
+
+/* Number of kernel launches this context has issued (for accounting). */
+int64_t ace_launch_count(const ace_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ACE_B200_H */

@@ -1,0 +1,181 @@
+"""GPU parity: libace_b200 (through its C ABI) against the FP64 CPU oracle.
+
+Tolerances (relative to the largest magnitude of the compared quantity):
+  FP64 mode: energies 1e-12, gradients 1e-10, basis 1e-12
+  FP32 mode: energies 1e-6 (the spec bar for the FP32 form), gradients 1e-4
+"""
+import numpy as np
+import pytest
+
+from ace_gb300.configs import random_batch
+from ace_gb300.spec import random_coefficients, symmetric_basis
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"fp64": dict(E=1e-12, G=1e-10, B=1e-12), "fp32": dict(E=1e-6, G=1e-4, B=1e-5)}
+
+
+def relerr(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def energy_relerr(E, Eref):
+    # per-environment relative error, normalised by |E| (floored at the rms energy)
+    scale = np.maximum(np.abs(Eref), np.sqrt(np.mean(Eref ** 2)))
+    return float(np.max(np.abs(E - Eref) / scale))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from ace_gb300 import lib as L
+    from ace_gb300.build import build
+    build()
+    return L
+
+
+SPECS = {
+    "test": dict(maxorder=3, maxdeg=6, maxL=6, rcut=5.0),
+    "cfg1": dict(maxorder=3, maxdeg=8, maxL=6),
+    "cfg2": dict(maxorder=4, maxdeg=12, maxL=12),
+    "ord5": dict(maxorder=5, maxdeg=10, maxL=10),
+}
+_spec_cache = {}
+
+
+def get_spec(name):
+    if name not in _spec_cache:
+        _spec_cache[name] = symmetric_basis(**SPECS[name])
+    return _spec_cache[name]
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("name,nenv,jlo,jhi", [("test", 64, 10, 10), ("cfg1", 1000, 12, 24),
+                                               ("cfg2", 200, 20, 60), ("ord5", 100, 20, 40)])
+def test_energy_forces(lib, oracle_mod, prec, name, nenv, jlo, jhi):
+    spec = get_spec(name)
+    c = random_coefficients(spec, seed=11)
+    b = random_batch(nenv, jlo, jhi, seed=5)
+    orc = oracle_mod.Oracle(spec, c)
+    Eref, Gref = orc.energy_forces(b.offsets, b.rr)
+    ctx = lib.Context(spec, prec)
+    ctx.set_params(c)
+    E, G = ctx.energy_forces(b.offsets, b.rr)
+    assert energy_relerr(E, Eref) <= TOL[prec]["E"], energy_relerr(E, Eref)
+    assert relerr(G, Gref) <= TOL[prec]["G"], relerr(G, Gref)
+    # energy-only entry point
+    E2 = ctx.energy_forces(b.offsets, b.rr, forces=False)
+    assert energy_relerr(E2, Eref) <= TOL[prec]["E"]
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_multispecies(lib, oracle_mod, prec):
+    spec = symmetric_basis(3, 6, maxL=6, nspecies=3)
+    c = random_coefficients(spec, seed=2)
+    b = random_batch(50, 8, 30, nspecies=3, seed=9)
+    orc = oracle_mod.Oracle(spec, c)
+    Eref, Gref = orc.energy_forces(b.offsets, b.rr, b.species)
+    ctx = lib.Context(spec, prec)
+    ctx.set_params(c)
+    E, G = ctx.energy_forces(b.offsets, b.rr, b.species)
+    assert energy_relerr(E, Eref) <= TOL[prec]["E"]
+    assert relerr(G, Gref) <= TOL[prec]["G"]
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_basis(lib, oracle_mod, prec):
+    spec = get_spec("cfg1")
+    b = random_batch(300, 12, 24, seed=4)
+    orc = oracle_mod.Oracle(spec)
+    Bref = orc.basis(b.offsets, b.rr)
+    ctx = lib.Context(spec, prec)
+    B = ctx.basis(b.offsets, b.rr)
+    assert relerr(B, Bref) <= TOL[prec]["B"]
+
+
+def test_edge_cases(lib, oracle_mod):
+    spec = get_spec("test")
+    c = random_coefficients(spec, seed=1)
+    ctx = lib.Context(spec, "fp64")
+    ctx.set_params(c)
+    ct = spec.ctilde(c)
+    # empty environments (the reference raises; here E = c~_0), ragged sizes, J = 1
+    offsets = np.array([0, 0, 1, 1, 4, 4], dtype=np.int64)
+    rr = np.random.default_rng(0).standard_normal((4, 3)) + 1.0
+    E, G = ctx.energy_forces(offsets, rr)
+    orc = oracle_mod.Oracle(spec, c)
+    for e in (1, 3):
+        o = slice(offsets[e], offsets[e + 1])
+        Er, Gr = orc.energy_forces(np.array([0, offsets[e + 1] - offsets[e]]), rr[o])
+        assert abs(E[e] - Er[0]) <= 1e-12 * max(1, abs(Er[0]))
+        assert np.allclose(G[o], Gr, rtol=1e-10, atol=1e-14)
+    for e in (0, 2, 4):
+        assert E[e] == ct[0]
+    # zero environments
+    E0, G0 = ctx.energy_forces(np.zeros(1, dtype=np.int64), np.zeros((0, 3)))
+    assert E0.shape == (0,)
+    # beyond the cutoff: R vanishes, only the constant remains
+    far = np.array([[6.0, 0.0, 0.0], [0.0, 7.0, 0.0]])
+    E1, G1 = ctx.energy_forces(np.array([0, 2]), far)
+    assert abs(E1[0] - ct[0]) < 1e-14 and np.all(G1 == 0)
+
+
+def test_invalid_inputs_rejected(lib):
+    spec = get_spec("test")
+    ctx = lib.Context(spec, "fp64")
+    rr = np.ones((3, 3))
+    with pytest.raises(lib.AceError):
+        ctx.energy_forces(np.array([0, 2, 1]), rr)          # non-monotone offsets
+    with pytest.raises(lib.AceError):
+        ctx.energy_forces(np.array([1, 3]), rr)             # offsets[0] != 0
+    bad = rr.copy(); bad[1, 0] = np.nan
+    with pytest.raises(lib.AceError):
+        ctx.energy_forces(np.array([0, 3]), bad)            # non-finite position
+    bad = rr.copy(); bad[2] = 0
+    with pytest.raises(lib.AceError):
+        ctx.energy_forces(np.array([0, 3]), bad)            # r == 0
+    with pytest.raises(lib.AceError):
+        ctx.set_params(np.zeros(spec.nB + 1))               # wrong length
+    spec3 = symmetric_basis(2, 4, maxL=4, nspecies=2)
+    ctx3 = lib.Context(spec3, "fp64")
+    with pytest.raises(lib.AceError):
+        ctx3.energy_forces(np.array([0, 3]), rr, np.array([0, 1, 2]))  # species out of range
+
+
+def test_device_pointer_path(lib, oracle_mod):
+    torch = pytest.importorskip("torch")
+    spec = get_spec("cfg1")
+    c = random_coefficients(spec, seed=3)
+    b = random_batch(500, 12, 24, seed=8)
+    orc = oracle_mod.Oracle(spec, c)
+    Eref, Gref = orc.energy_forces(b.offsets, b.rr)
+    ctx = lib.Context(spec, "fp64")
+    ctx.set_params(c)
+    off = torch.from_numpy(b.offsets).cuda()
+    rr = torch.from_numpy(b.rr).cuda()
+    E = torch.empty(b.nenv, dtype=torch.float64, device="cuda")
+    G = torch.empty_like(rr)
+    stream = torch.cuda.current_stream().cuda_stream
+    ctx.energy_forces_device(off, rr, None, E, G, stream=stream, sync=False)
+    ctx.sync()
+    assert energy_relerr(E.cpu().numpy(), Eref) <= 1e-12
+    assert relerr(G.cpu().numpy(), Gref) <= 1e-10
+
+
+def test_model_api(lib, oracle_mod):
+    from ace_gb300.model import LinearACEModel, SymmetricBasis
+    basis = SymmetricBasis(spec=get_spec("test"))
+    c = random_coefficients(basis.spec, seed=5)
+    model = LinearACEModel(basis, c)
+    b = random_batch(5, 10, 10, seed=6)
+    cfgs = [b.env(e)[0] for e in range(5)]
+    E = model.evaluate(cfgs)
+    orc = oracle_mod.Oracle(basis.spec, c)
+    assert np.allclose(E, orc.evaluate(b.offsets, b.rr), rtol=1e-12)
+    assert np.isclose(model.evaluate(cfgs[0]), E[0], rtol=1e-14)
+    g = model.grad_config(cfgs)
+    assert np.allclose(np.concatenate(g), orc.grad_config(b.offsets, b.rr), rtol=1e-10, atol=1e-14)
+    B = model.grad_params(cfgs)
+    assert np.allclose(B @ c, E, rtol=1e-12)
+    c2 = random_coefficients(basis.spec, seed=7)
+    model.set_params(c2)
+    assert np.allclose(model.evaluate(cfgs), B @ c2, rtol=1e-11)
