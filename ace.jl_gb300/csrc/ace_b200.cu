@@ -11,7 +11,8 @@
 
 #include "../../include/ace_b200.h"
 #include "ace_ctx.h"
-#include "ace_kernels.cuh"
+#include "ace_phi.cuh"
+#include "ace_sched.h"
 
 using namespace ace;
 
@@ -39,10 +40,14 @@ template <typename T> static int upload(ace_ctx *ctx, T **dst, const T *src, siz
   return ACE_OK;
 }
 
-static void alp_tables(int L, std::vector<double> &A, std::vector<double> &B) {
-  int sz = size_p(L);
-  A.assign(sz, 0.0);
-  B.assign(sz, 0.0);
+// Coefficient table (layout documented in ace_phi.cuh).
+static std::vector<double> coef_table(const ace_spec_bundle *s, int L) {
+  const int szP = size_p(L);
+  std::vector<double> t;
+  t.insert(t.end(), s->rA, s->rA + s->nR);
+  t.insert(t.end(), s->rB, s->rB + s->nR);
+  t.insert(t.end(), s->rC, s->rC + s->nR);
+  std::vector<double> A(szP, 0.0), B(szP, 0.0), C(L + 1, 0.0), D(L + 1, 0.0);
   for (int l = 2; l <= L; ++l) {
     double ls = double(l * l), lm1s = double((l - 1) * (l - 1));
     for (int m = 0; m <= l - 2; ++m) {
@@ -50,7 +55,17 @@ static void alp_tables(int L, std::vector<double> &A, std::vector<double> &B) {
       A[idx_p(l, m)] = std::sqrt((4 * ls - 1.0) / (ls - ms));
       B[idx_p(l, m)] = -std::sqrt((lm1s - ms) / (4 * lm1s - 1.0));
     }
+    C[l] = std::sqrt(double(2 * (l - 1) + 3));
+    D[l] = -std::sqrt(1.0 + 0.5 / l);
   }
+  t.insert(t.end(), A.begin(), A.end());
+  t.insert(t.end(), B.begin(), B.end());
+  t.insert(t.end(), C.begin(), C.end());
+  t.insert(t.end(), D.begin(), D.end());
+  const double k[7] = {s->tl, s->tr, 1.0 + s->r0, std::sqrt(3.0), std::sqrt(1.5), std::sqrt(0.5 / M_PI),
+                       1.0 / std::sqrt(2.0)};
+  t.insert(t.end(), k, k + 7);
+  return t;
 }
 
 static int validate_spec(const ace_spec_bundle *s, std::string &why) {
@@ -71,7 +86,7 @@ static int validate_spec(const ace_spec_bundle *s, std::string &why) {
     if (s->a_m[i] < -s->a_l[i] || s->a_m[i] > s->a_l[i]) { why = "|a_m| > a_l"; return ACE_ERR_INVALID; }
     if (s->a_mu && (s->a_mu[i] < 0 || s->a_mu[i] >= s->nspecies)) { why = "a_mu out of range"; return ACE_ERR_INVALID; }
   }
-  if (s->nAA < 1 || s->maxord < 1 || s->maxord > ACE_MAX_ORD) { why = "nAA/maxord out of range (maxord <= 8)"; return ACE_ERR_UNSUPPORTED; }
+  if (s->nAA < 1 || s->maxord < 1 || s->maxord > ACE_MAX_ORD) { why = "nAA/maxord out of range (maxord <= 6)"; return ACE_ERR_UNSUPPORTED; }
   if (!s->orders || !s->iAA2iA) { why = "AA spec arrays missing"; return ACE_ERR_INVALID; }
   for (int64_t k = 0; k < s->nAA; ++k) {
     int o = s->orders[k];
@@ -100,7 +115,7 @@ extern "C" int ace_ctx_create(const ace_spec_bundle *s, int32_t prec, int32_t de
   std::string why;
   int rc = validate_spec(s, why);
   if (rc != ACE_OK) return ctx_fail(nullptr, rc, why);
-  if (prec != ACE_PREC_FP64 && prec != ACE_PREC_FP32 && prec != ACE_PREC_FP32_BF16X3)
+  if (prec != ACE_PREC_FP64 && prec != ACE_PREC_FP32 && prec != ACE_PREC_FP32_BF16X3 && prec != ACE_PREC_FP32X2)
     return ctx_fail(nullptr, ACE_ERR_UNSUPPORTED, "precision mode not supported");
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev)
@@ -122,16 +137,15 @@ extern "C" int ace_ctx_create(const ace_spec_bundle *s, int32_t prec, int32_t de
   ctx->nsm = prop.multiProcessorCount;
   ctx->smem_optin = (int)prop.sharedMemPerBlockOptin;
 
-  // coefficient tables: rA rB rC (nR) alpA alpB (szP), in double and float
-  std::vector<double> alpA, alpB;
-  alp_tables(L, alpA, alpB);
-  std::vector<double> tabD;
-  tabD.insert(tabD.end(), s->rA, s->rA + s->nR);
-  tabD.insert(tabD.end(), s->rB, s->rB + s->nR);
-  tabD.insert(tabD.end(), s->rC, s->rC + s->nR);
-  tabD.insert(tabD.end(), alpA.begin(), alpA.end());
-  tabD.insert(tabD.end(), alpB.begin(), alpB.end());
+  // coefficient tables in double, float and double-float
+  std::vector<double> tabD = coef_table(s, L);
   std::vector<float> tabF(tabD.begin(), tabD.end());
+  std::vector<float> tabDF(2 * tabD.size());
+  for (size_t i = 0; i < tabD.size(); ++i) {
+    float h = (float)tabD[i];
+    tabDF[2 * i] = h;
+    tabDF[2 * i + 1] = (float)(tabD[i] - (double)h);
+  }
   ctx->ntab = (int)tabD.size();
   // A spec
   std::vector<int16_t> an(s->nA), aiy(s->nA), amu(s->nA, 0);
@@ -140,7 +154,7 @@ extern "C" int ace_ctx_create(const ace_spec_bundle *s, int32_t prec, int32_t de
     aiy[i] = (int16_t)idx_y(s->a_l[i], s->a_m[i]);
     if (s->a_mu) amu[i] = (int16_t)s->a_mu[i];
   }
-  // AA spec: orders (uint8) and SoA indices idx[t * nAA + k] (uint16)
+  // AA spec for the flat-product (basis) path: orders and SoA indices idx[t * nAA + k]
   std::vector<uint8_t> ord(s->nAA);
   std::vector<uint16_t> idx((size_t)s->maxord * s->nAA, 0);
   for (int64_t k = 0; k < s->nAA; ++k) {
@@ -150,6 +164,7 @@ extern "C" int ace_ctx_create(const ace_spec_bundle *s, int32_t prec, int32_t de
   ctx->has_const = (s->orders[0] == 0);
   if ((rc = upload(ctx, &ctx->d_tabD, tabD.data(), tabD.size())) ||
       (rc = upload(ctx, &ctx->d_tabF, tabF.data(), tabF.size())) ||
+      (rc = upload(ctx, &ctx->d_tabDF, tabDF.data(), tabDF.size())) ||
       (rc = upload(ctx, &ctx->d_an, an.data(), an.size())) ||
       (rc = upload(ctx, &ctx->d_aiy, aiy.data(), aiy.size())) ||
       (rc = upload(ctx, &ctx->d_amu, amu.data(), amu.size())) ||
@@ -157,6 +172,30 @@ extern "C" int ace_ctx_create(const ace_spec_bundle *s, int32_t prec, int32_t de
       (rc = upload(ctx, &ctx->d_idx, idx.data(), idx.size()))) {
     g_create_error = ctx->err;
     return fail(rc);
+  }
+  // correlation schedule
+  {
+    Schedule sch = build_schedule(s->nA, s->a_n, s->a_l, s->a_m, s->a_mu, s->nAA, s->maxord, s->orders,
+                                  s->iAA2iA, s->nB, s->U_indptr, s->U_indices, s->U_data, ctx->nt);
+    ctx->sn = sch.n;
+    ctx->halved = sch.halved;
+    ctx->sched_nodes = sch.nodes;
+    ctx->sk = sch.k;
+    ctx->sw = sch.w;
+    if ((rc = upload(ctx, &ctx->d_sv, sch.v.data(), sch.v.size())) ||
+        (rc = upload(ctx, &ctx->d_sord, sch.ord.data(), sch.ord.size())) ||
+        (rc = upload(ctx, &ctx->d_sq, sch.q.data(), sch.q.size())) ||
+        (rc = upload(ctx, &ctx->d_sstart, sch.start.data(), sch.start.size()))) {
+      g_create_error = ctx->err;
+      return fail(rc);
+    }
+    const size_t csz = (prec == ACE_PREC_FP64) ? 8 : (prec == ACE_PREC_FP32X2 ? 8 : 4);
+    if (cudaMalloc(&ctx->d_sc, std::max<int64_t>(sch.n, 1) * csz) != cudaSuccess) {
+      g_create_error = "cudaMalloc failed";
+      return fail(ACE_ERR_ALLOC);
+    }
+    ctx->allocs.push_back(ctx->d_sc);
+    cudaMemset(ctx->d_sc, 0, std::max<int64_t>(sch.n, 1) * csz);
   }
   // U (host copy for c~ = U^T c; device copy for the basis path)
   if (s->nB > 0) {
@@ -173,18 +212,12 @@ extern "C" int ace_ctx_create(const ace_spec_bundle *s, int32_t prec, int32_t de
       return fail(rc);
     }
   }
-  // coefficients (zero) and status word
-  if (cudaMalloc((void **)&ctx->d_ctD, s->nAA * sizeof(double)) != cudaSuccess ||
-      cudaMalloc((void **)&ctx->d_ctF, s->nAA * sizeof(float)) != cudaSuccess ||
-      cudaMalloc((void **)&ctx->d_status, sizeof(int)) != cudaSuccess) {
+  // status word
+  if (cudaMalloc((void **)&ctx->d_status, sizeof(int)) != cudaSuccess) {
     g_create_error = "cudaMalloc failed";
     return fail(ACE_ERR_ALLOC);
   }
-  ctx->allocs.push_back(ctx->d_ctD);
-  ctx->allocs.push_back(ctx->d_ctF);
   ctx->allocs.push_back(ctx->d_status);
-  cudaMemset(ctx->d_ctD, 0, s->nAA * sizeof(double));
-  cudaMemset(ctx->d_ctF, 0, s->nAA * sizeof(float));
   cudaMemset(ctx->d_status, 0, sizeof(int));
   ctx->ctilde.assign(s->nAA, 0.0);
   if (cudaMallocHost((void **)&ctx->h_status, sizeof(int)) != cudaSuccess) {
@@ -210,11 +243,30 @@ extern "C" int ace_ctx_destroy(ace_ctx *ctx) {
   return ACE_OK;
 }
 
+// Pack w * c~ in schedule order, in the energy type of the precision mode.
 static int push_ctilde(ace_ctx *ctx) {
-  std::vector<float> f(ctx->ctilde.begin(), ctx->ctilde.end());
   ACE_CUDA(cudaSetDevice(ctx->device));
-  ACE_CUDA(cudaMemcpy(ctx->d_ctD, ctx->ctilde.data(), ctx->nAA * sizeof(double), cudaMemcpyHostToDevice));
-  ACE_CUDA(cudaMemcpy(ctx->d_ctF, f.data(), ctx->nAA * sizeof(float), cudaMemcpyHostToDevice));
+  const int64_t n = ctx->sn;
+  if (n > 0) {
+    if (ctx->prec == ACE_PREC_FP64) {
+      std::vector<double> c(n);
+      for (int64_t i = 0; i < n; ++i) c[i] = ctx->sw[i] * ctx->ctilde[ctx->sk[i]];
+      ACE_CUDA(cudaMemcpy(ctx->d_sc, c.data(), n * 8, cudaMemcpyHostToDevice));
+    } else if (ctx->prec == ACE_PREC_FP32X2) {
+      std::vector<float> c(2 * n);
+      for (int64_t i = 0; i < n; ++i) {
+        const double v = ctx->sw[i] * ctx->ctilde[ctx->sk[i]];
+        const float h = (float)v;
+        c[2 * i] = h;
+        c[2 * i + 1] = (float)(v - (double)h);
+      }
+      ACE_CUDA(cudaMemcpy(ctx->d_sc, c.data(), n * 8, cudaMemcpyHostToDevice));
+    } else {
+      std::vector<float> c(n);
+      for (int64_t i = 0; i < n; ++i) c[i] = (float)(ctx->sw[i] * ctx->ctilde[ctx->sk[i]]);
+      ACE_CUDA(cudaMemcpy(ctx->d_sc, c.data(), n * 4, cudaMemcpyHostToDevice));
+    }
+  }
   return ACE_OK;
 }
 

@@ -8,7 +8,7 @@
 
 #define ACE_MAX_NR 32
 #define ACE_MAX_L 20
-#define ACE_MAX_ORD 8
+#define ACE_MAX_ORD 6
 
 // device status word bits (set by kernels, read back by the host)
 #define ACE_STATUS_BAD_OFFSETS 1
@@ -25,19 +25,29 @@ struct ace_ctx {
   bool has_const = false;
 
   // device copies of the spec
-  double *d_tabD = nullptr;   // rA rB rC alpA alpB
-  float *d_tabF = nullptr;
+  double *d_tabD = nullptr;   // coefficient tables (table_size entries) in double,
+  float *d_tabF = nullptr;    // float,
+  float *d_tabDF = nullptr;   // and double-float pairs
   int16_t *d_an = nullptr, *d_aiy = nullptr, *d_amu = nullptr;
   uint8_t *d_ord = nullptr;
-  uint16_t *d_idx = nullptr;  // [maxord][nAA]
-  double *d_ctD = nullptr;
-  float *d_ctF = nullptr;
+  uint16_t *d_idx = nullptr;  // [maxord][nAA], flat products (basis path)
   int64_t *d_Uptr = nullptr;
   int32_t *d_Uidx = nullptr;
   double *d_UvalD = nullptr;
   float *d_UvalF = nullptr;
   int *d_status = nullptr;
   int *h_status = nullptr;
+
+  // correlation schedule (ace_sched.h)
+  int64_t sn = 0;
+  bool halved = false;
+  int64_t sched_nodes = 0;
+  uint16_t *d_sv = nullptr;
+  uint8_t *d_sord = nullptr, *d_sq = nullptr;
+  int32_t *d_sstart = nullptr;
+  void *d_sc = nullptr;        // packed coefficients in the energy type
+  std::vector<int32_t> sk;     // schedule -> AA index
+  std::vector<uint8_t> sw;     // weights
 
   // host copies
   std::vector<double> ctilde;
@@ -52,8 +62,10 @@ struct ace_ctx {
   size_t scratch_bytes = 0;
 
   // launch configuration chosen at create time
-  int ef_block = 256, ef_chunk = 32, ef_grid = 0;
-  size_t ef_smem = 0;
+  int nt = 128, chunkE = 32, chunkG = 16, npriv = 32, grid = 0;
+  size_t smem = 0;
+  int aa_chunk = 32, aa_grid = 0;
+  size_t aa_smem = 0;
 
   std::vector<void *> allocs;
   int64_t launches = 0;

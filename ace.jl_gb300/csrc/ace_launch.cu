@@ -1,0 +1,176 @@
+// ace_launch.cu -- launch configuration and dispatch of the evaluation kernels.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "../../include/ace_b200.h"
+#include "ace_ctx.h"
+#include "ace_kernels.cuh"
+
+namespace ace {
+
+static constexpr int NT = 128;  // threads per CTA of the energy/forces kernel
+
+template <typename TE, typename TG, bool GRAD>
+static void *ef_func_k(int K) {
+  switch (K) {
+    case 1:
+    case 2: return (void *)ef_kernel<TE, TG, 2, NT, GRAD>;
+    case 3: return (void *)ef_kernel<TE, TG, 3, NT, GRAD>;
+    case 4: return (void *)ef_kernel<TE, TG, 4, NT, GRAD>;
+    case 5: return (void *)ef_kernel<TE, TG, 5, NT, GRAD>;
+    default: return (void *)ef_kernel<TE, TG, 6, NT, GRAD>;
+  }
+}
+
+static void *ef_func(const ace_ctx *ctx, bool grad) {
+  switch (ctx->prec) {
+    case ACE_PREC_FP64: return grad ? ef_func_k<double, double, true>(ctx->maxord) : ef_func_k<double, double, false>(ctx->maxord);
+    case ACE_PREC_FP32X2: return grad ? ef_func_k<df, float, true>(ctx->maxord) : ef_func_k<df, float, false>(ctx->maxord);
+    default: return grad ? ef_func_k<float, float, true>(ctx->maxord) : ef_func_k<float, float, false>(ctx->maxord);
+  }
+}
+
+static void *aa_func(const ace_ctx *ctx) {
+  switch (ctx->prec) {
+    case ACE_PREC_FP64: return (void *)aa_kernel<double, double>;
+    case ACE_PREC_FP32X2: return (void *)aa_kernel<df, double>;
+    default: return (void *)aa_kernel<float, float>;
+  }
+}
+
+static void type_sizes(const ace_ctx *ctx, int &sE, int &sG, bool &same) {
+  switch (ctx->prec) {
+    case ACE_PREC_FP64: sE = 8; sG = 8; same = true; break;
+    case ACE_PREC_FP32X2: sE = 8; sG = 4; same = false; break;
+    default: sE = 4; sG = 4; same = true; break;
+  }
+}
+
+int kernels_prepare(ace_ctx *ctx) {
+  int sE, sG;
+  bool same;
+  type_sizes(ctx, sE, sG, same);
+  ctx->nt = NT;
+  // neighbour chunks of ~32 KB slabs each; private adjoint bins in ~32 KB
+  const int slabE = (ctx->nR + size_p(ctx->L) + 2 * size_y(ctx->L)) * sE;
+  const int slabG = (2 * ctx->nR + 2 * size_p(ctx->L) + 8 * size_y(ctx->L)) * sG;
+  ctx->chunkE = std::max(1, std::min(64, (32 * 1024) / slabE));
+  ctx->chunkG = std::max(1, std::min(32, (32 * 1024) / slabG));
+  ctx->npriv = std::max(1, std::min(ctx->nA, (32 * 1024) / (NT * 2 * sG)));
+  EFLayout lay = ef_layout(ctx->ntab, ctx->nR, ctx->L, ctx->nA, ctx->chunkE, ctx->chunkG, ctx->npriv, NT, sE, sG, same);
+  while (lay.total > (size_t)ctx->smem_optin && (ctx->chunkE > 1 || ctx->chunkG > 1 || ctx->npriv > 1)) {
+    ctx->chunkE = std::max(1, ctx->chunkE / 2);
+    ctx->chunkG = std::max(1, ctx->chunkG / 2);
+    ctx->npriv = std::max(1, ctx->npriv / 2);
+    lay = ef_layout(ctx->ntab, ctx->nR, ctx->L, ctx->nA, ctx->chunkE, ctx->chunkG, ctx->npriv, NT, sE, sG, same);
+  }
+  if (lay.total > (size_t)ctx->smem_optin) {
+    ctx->err = "spec too large for shared memory";
+    return ACE_ERR_UNSUPPORTED;
+  }
+  ctx->smem = lay.total;
+  int occ = 1;
+  for (int g = 0; g < 2; ++g) {
+    void *f = ef_func(ctx, g == 1);
+    if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lay.total) != cudaSuccess) {
+      ctx->err = "cudaFuncSetAttribute failed";
+      return ACE_ERR_CUDA;
+    }
+    if (g == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, f, NT, lay.total);
+  }
+  ctx->grid = ctx->nsm * std::max(occ, 1);
+  // basis path (AA materialisation)
+  ctx->aa_chunk = std::max(1, std::min(64, (32 * 1024) / slabE));
+  EFLayout la = ef_layout(ctx->ntab, ctx->nR, ctx->L, ctx->nA, ctx->aa_chunk, 1, 0, 256, sE, sE, true);
+  ctx->aa_smem = la.total;
+  void *fa = aa_func(ctx);
+  if (cudaFuncSetAttribute(fa, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)la.total) != cudaSuccess) {
+    ctx->err = "cudaFuncSetAttribute failed";
+    return ACE_ERR_CUDA;
+  }
+  int occa = 1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occa, fa, 256, la.total);
+  ctx->aa_grid = ctx->nsm * std::max(occa, 1);
+  return ACE_OK;
+}
+
+static EFArgs make_args(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const double *rr, const int32_t *sp,
+                        double *E, double *G) {
+  EFArgs a{};
+  a.nEnv = nEnv; a.off = off; a.rr = rr; a.sp = sp; a.E = E; a.G = G;
+  switch (ctx->prec) {
+    case ACE_PREC_FP64: a.tabE = ctx->d_tabD; a.tabG = ctx->d_tabD; break;
+    case ACE_PREC_FP32X2: a.tabE = ctx->d_tabDF; a.tabG = ctx->d_tabF; break;
+    default: a.tabE = ctx->d_tabF; a.tabG = ctx->d_tabF; break;
+  }
+  a.ntab = ctx->ntab; a.nR = ctx->nR; a.L = ctx->L; a.pl = ctx->pl; a.pr = ctx->pr; a.tp = ctx->tp;
+  a.an = ctx->d_an; a.aiy = ctx->d_aiy; a.amu = ctx->d_amu;
+  a.nA = ctx->nA; a.nspecies = ctx->nspecies;
+  a.sv = ctx->d_sv; a.sord = ctx->d_sord; a.sq = ctx->d_sq; a.sc = ctx->d_sc; a.sn = ctx->sn;
+  a.sstart = ctx->d_sstart;
+  a.c0 = ctx->has_const ? ctx->ctilde[0] : 0.0;
+  a.chunkE = ctx->chunkE; a.chunkG = ctx->chunkG; a.npriv = ctx->npriv;
+  a.status = ctx->d_status;
+  a.ord = ctx->d_ord; a.idx = ctx->d_idx; a.nAA = ctx->nAA;
+  return a;
+}
+
+int launch_energy_forces(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const double *rr, const int32_t *sp,
+                         double *E, double *G, cudaStream_t st) {
+  if (nEnv == 0) return ACE_OK;
+  EFArgs a = make_args(ctx, nEnv, off, rr, sp, E, G);
+  void *f = ef_func(ctx, G != nullptr);
+  const int grid = (int)std::min<int64_t>(nEnv, ctx->grid);
+  void *args[] = {&a};
+  cudaError_t e = cudaLaunchKernel(f, dim3(grid), dim3(NT), args, ctx->smem, st);
+  ctx->launches += 1;
+  if (e != cudaSuccess) { ctx->err = cudaGetErrorString(e); return ACE_ERR_CUDA; }
+  return ACE_OK;
+}
+
+static int ensure_scratch(ace_ctx *ctx, size_t bytes) {
+  if (bytes <= ctx->scratch_bytes) return ACE_OK;
+  if (ctx->d_scratch) { cudaFree(ctx->d_scratch); ctx->d_scratch = nullptr; ctx->scratch_bytes = 0; }
+  if (cudaMalloc(&ctx->d_scratch, bytes) != cudaSuccess) { ctx->err = "scratch allocation failed"; return ACE_ERR_ALLOC; }
+  ctx->scratch_bytes = bytes;
+  return ACE_OK;
+}
+
+int launch_basis(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const double *rr, const int32_t *sp,
+                 double *B, double *dB, cudaStream_t st) {
+  if (dB) { ctx->err = "dB is not produced by this build"; return ACE_ERR_UNSUPPORTED; }
+  if (nEnv == 0) return ACE_OK;
+  const bool f32 = (ctx->prec == ACE_PREC_FP32 || ctx->prec == ACE_PREC_FP32_BF16X3);
+  const size_t ts = f32 ? 4 : 8;
+  int64_t per = std::max<int64_t>(1, (int64_t)((512ull << 20) / (ctx->nAA * ts)));
+  per = std::min<int64_t>(per, nEnv);
+  int rc = ensure_scratch(ctx, (size_t)per * ctx->nAA * ts);
+  if (rc) return rc;
+  void *fa = aa_func(ctx);
+  for (int64_t e0 = 0; e0 < nEnv; e0 += per) {
+    const int64_t ne = std::min(per, nEnv - e0);
+    EFArgs a = make_args(ctx, ne, off + e0, rr, sp, nullptr, nullptr);
+    a.chunkE = ctx->aa_chunk;
+    a.AAout = ctx->d_scratch;
+    a.ldE = ne;
+    const int grid = (int)std::min<int64_t>(ne, ctx->aa_grid);
+    void *args[] = {&a};
+    cudaError_t err = cudaLaunchKernel(fa, dim3(grid), dim3(256), args, ctx->aa_smem, st);
+    ctx->launches += 1;
+    if (err != cudaSuccess) { ctx->err = cudaGetErrorString(err); return ACE_ERR_CUDA; }
+    dim3 g2((unsigned)((ne + 127) / 128), (unsigned)std::min<int64_t>(ctx->nB, 65535));
+    if (!f32)
+      ub_kernel<double><<<g2, 128, 0, st>>>(ne, e0, ne, ctx->nB, ctx->d_Uptr, ctx->d_Uidx, ctx->d_UvalD,
+                                             (const double *)ctx->d_scratch, B);
+    else
+      ub_kernel<float><<<g2, 128, 0, st>>>(ne, e0, ne, ctx->nB, ctx->d_Uptr, ctx->d_Uidx, ctx->d_UvalF,
+                                            (const float *)ctx->d_scratch, B);
+    ctx->launches += 1;
+    err = cudaGetLastError();
+    if (err != cudaSuccess) { ctx->err = cudaGetErrorString(err); return ACE_ERR_CUDA; }
+  }
+  return ACE_OK;
+}
+
+}  // namespace ace

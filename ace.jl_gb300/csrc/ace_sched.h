@@ -1,0 +1,144 @@
+// ace_sched.h -- host-side preparation of the correlation (AA) evaluation
+// schedule consumed by the trie kernel.
+//
+// The reference evaluates each AA function as a flat product
+// (src/evaluator.jl:137-142, src/pibasis.jl:265-275).  Here the functions are
+// visited in lexicographic order of their (descending) index tuples, so that
+// functions sharing a prefix (v1, ..., vd) are adjacent: the kernel keeps the
+// prefix products and Horner partial sums of the current path in registers,
+// which is the recursive product evaluation of src/grapheval.jl:80-278
+// restricted to prefix splits.
+//
+// Conjugation symmetry: for real positions A_{n,l,-m} = (-1)^m conj(A_{n,l,m}),
+// so AA of the m-reversed tuple is the complex conjugate (sum m = 0), and the
+// invariant coupling gives both the same c~.  Only one function of each such
+// pair is kept, with weight 2; the same weights give the correct adjoint for
+// the forces (the partner's contribution to Re(dAco . dA) is identical).  The
+// halving is used only if every partner exists and U has identical columns
+// for both partners.
+#pragma once
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <map>
+#include <numeric>
+#include <vector>
+
+namespace ace {
+
+struct Schedule {
+  int K = 0;                       // maximum order
+  int64_t n = 0;                   // scheduled functions (order >= 1)
+  std::vector<uint16_t> v;         // [K][n] indices (descending within a function)
+  std::vector<uint8_t> ord;        // [n]
+  std::vector<uint8_t> q;          // [n] common prefix length with the previous function
+  std::vector<int32_t> k;          // [n] index of the AA function in the spec
+  std::vector<uint8_t> w;          // [n] weight (1, or 2 for a conjugate pair)
+  std::vector<int32_t> start;      // [nthreads + 1] per-thread ranges
+  bool halved = false;
+  int64_t nodes = 0;               // trie nodes opened (for accounting)
+};
+
+inline Schedule build_schedule(int nA, const int32_t *a_n, const int32_t *a_l, const int32_t *a_m,
+                               const int32_t *a_mu, int64_t nAA, int K, const int32_t *orders,
+                               const int32_t *iAA2iA, int64_t nB, const int64_t *U_indptr,
+                               const int32_t *U_indices, const double *U_data, int nthreads) {
+  Schedule s;
+  s.K = K;
+  // ---- partner A indices (m -> -m)
+  std::map<std::tuple<int, int, int, int>, int> aidx;
+  for (int i = 0; i < nA; ++i) aidx[{a_mu ? a_mu[i] : 0, a_n[i], a_l[i], a_m[i]}] = i;
+  std::vector<int> partner(nA, -1);
+  bool ok = true;
+  for (int i = 0; i < nA; ++i) {
+    auto it = aidx.find({a_mu ? a_mu[i] : 0, a_n[i], a_l[i], -a_m[i]});
+    if (it == aidx.end()) { ok = false; break; }
+    partner[i] = it->second;
+  }
+  // ---- partner AA functions
+  std::map<std::vector<int>, int64_t> tidx;
+  for (int64_t k = 0; k < nAA; ++k) {
+    std::vector<int> t(iAA2iA + k * K, iAA2iA + k * K + orders[k]);
+    tidx[t] = k;
+  }
+  std::vector<int64_t> pk(nAA, -1);
+  if (ok) {
+    for (int64_t k = 0; k < nAA && ok; ++k) {
+      std::vector<int> t;
+      for (int j = 0; j < orders[k]; ++j) t.push_back(partner[iAA2iA[k * K + j]]);
+      std::sort(t.begin(), t.end(), std::greater<int>());
+      auto it = tidx.find(t);
+      if (it == tidx.end()) { ok = false; break; }
+      pk[k] = it->second;
+    }
+  }
+  // ---- U columns of partners must agree (then c~ agrees for every c)
+  if (ok && nB > 0) {
+    std::vector<std::vector<std::pair<int64_t, double>>> cols(nAA);
+    for (int64_t b = 0; b < nB; ++b)
+      for (int64_t j = U_indptr[b]; j < U_indptr[b + 1]; ++j) cols[U_indices[j]].push_back({b, U_data[j]});
+    for (int64_t k = 0; k < nAA && ok; ++k) {
+      const auto &a = cols[k], &b = cols[pk[k]];
+      if (a.size() != b.size()) { ok = false; break; }
+      for (size_t j = 0; j < a.size(); ++j)
+        if (a[j].first != b[j].first || std::fabs(a[j].second - b[j].second) > 1e-12 * (1.0 + std::fabs(a[j].second))) {
+          ok = false; break;
+        }
+    }
+  }
+  s.halved = ok;
+  // ---- kept functions (order >= 1)
+  std::vector<int64_t> keep;
+  std::vector<uint8_t> wts;
+  for (int64_t k = 0; k < nAA; ++k) {
+    if (orders[k] == 0) continue;
+    if (ok) {
+      if (pk[k] == k) { keep.push_back(k); wts.push_back(1); }
+      else if (pk[k] > k) { keep.push_back(k); wts.push_back(2); }
+    } else {
+      keep.push_back(k); wts.push_back(1);
+    }
+  }
+  // ---- lexicographic order of the descending tuples (prefix first)
+  std::vector<size_t> perm(keep.size());
+  std::iota(perm.begin(), perm.end(), 0);
+  auto tup = [&](size_t i) { const int64_t k = keep[i]; return std::vector<int>(iAA2iA + k * K, iAA2iA + k * K + orders[k]); };
+  std::vector<std::vector<int>> tuples(keep.size());
+  for (size_t i = 0; i < keep.size(); ++i) tuples[i] = tup(i);
+  std::stable_sort(perm.begin(), perm.end(), [&](size_t a, size_t b) { return tuples[a] < tuples[b]; });
+  s.n = (int64_t)keep.size();
+  s.v.assign((size_t)K * s.n, 0);
+  s.ord.resize(s.n); s.q.resize(s.n); s.k.resize(s.n); s.w.resize(s.n);
+  std::vector<double> cost(s.n);
+  for (int64_t i = 0; i < s.n; ++i) {
+    const auto &t = tuples[perm[i]];
+    s.ord[i] = (uint8_t)t.size();
+    s.k[i] = (int32_t)keep[perm[i]];
+    s.w[i] = wts[perm[i]];
+    for (size_t j = 0; j < t.size(); ++j) s.v[(size_t)j * s.n + i] = (uint16_t)t[j];
+    int qq = 0;
+    if (i > 0) {
+      const auto &p = tuples[perm[i - 1]];
+      while (qq < (int)std::min(p.size(), t.size()) && p[qq] == t[qq]) ++qq;
+    }
+    s.q[i] = (uint8_t)qq;
+    cost[i] = 1.0 + 2.0 * (double)(t.size() - qq);
+  }
+  // ---- balanced contiguous ranges
+  s.start.assign(nthreads + 1, 0);
+  const double total = std::accumulate(cost.begin(), cost.end(), 0.0);
+  double acc = 0.0;
+  int th = 1;
+  for (int64_t i = 0; i < s.n && th < nthreads; ++i) {
+    acc += cost[i];
+    while (th < nthreads && acc >= total * th / nthreads) s.start[th++] = (int32_t)(i + 1);
+  }
+  while (th <= nthreads) s.start[th++] = (int32_t)s.n;
+  // a range starts from an empty path
+  for (int t = 0; t < nthreads; ++t)
+    if (s.start[t] < s.n) s.q[s.start[t]] = 0;
+  for (int64_t i = 0; i < s.n; ++i) s.nodes += s.ord[i] - s.q[i];
+  return s;
+}
+
+}  // namespace ace

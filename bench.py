@@ -30,6 +30,7 @@ sys.path.insert(0, os.path.join(ROOT, "ace.jl_gb300"))
 
 METRIC = "env-evals/s (E+F) on 1 GB300: chosen form vs plain FP64 path at <=1e-6 rel err"
 UNIT = "env/s"
+CHOSEN = "fp32x2"
 WORKLOAD = dict(name="ace-invariant ord4 deg12 L12, 100k envs, J~U{20..60}",
                 maxorder=4, maxdeg=12, maxL=12, nenv=100_000, jlo=20, jhi=60, seed=2024)
 
@@ -269,18 +270,26 @@ def main():
     k64 = max(1, min(args.steps, 3))
     t64, _ = timed(ctx64, k64, min(args.warmup, 1))
     E64 = E_d.cpu().numpy().copy(); G64 = G_d.cpu().numpy().copy()
-    # the chosen form: FP32
-    ctx = Context(spec, "fp32", device=local)
+    scale = np.maximum(np.abs(E64), np.sqrt(np.mean(E64 ** 2)))
+
+    def errors():
+        E = E_d.cpu().numpy(); G = G_d.cpu().numpy()
+        return {"E_rel_max_vs_fp64": float(np.max(np.abs(E - E64) / scale)),
+                "F_rel_max_vs_fp64": float(np.max(np.abs(G - G64)) / np.max(np.abs(G64)))}
+    # plain FP32 (fast, not within the 1e-6 bar)
+    ctx32 = Context(spec, "fp32", device=local)
+    ctx32.set_params(c)
+    t32p, _ = timed(ctx32, args.steps, args.warmup)
+    err32 = errors()
+    # the chosen form: double-float energy path, FP32 adjoint and forces
+    ctx = Context(spec, CHOSEN, device=local)
     ctx.set_params(c)
     with Clocks(local) as clk:
         t32, launches = timed(ctx, args.steps, args.warmup)
     clocks = clk.summary()
-    E32 = E_d.cpu().numpy(); G32 = G_d.cpu().numpy()
+    err = errors()
     value = nenv * args.steps * world / t32
     ms = 1e3 * t32 / args.steps
-    scale = np.maximum(np.abs(E64), np.sqrt(np.mean(E64 ** 2)))
-    err = {"E_rel_max_vs_fp64": float(np.max(np.abs(E32 - E64) / scale)),
-           "F_rel_max_vs_fp64": float(np.max(np.abs(G32 - G64)) / np.max(np.abs(G64)))}
 
     # e2e through the C ABI with pinned host buffers
     e2e = None
@@ -327,18 +336,20 @@ def main():
         traffic = tr["dram_bytes_per_env"] * nenv
     roof = {"bound": "fp32", "achieved": achieved, "peak": peaks["fp32_tflops"], "unit": "TFLOP/s",
             "frac": achieved / peaks["fp32_tflops"], "traffic": traffic,
-            "kernel": "ef_kernel<float> (fused 1p basis, A, AA, adjoint, forces)",
+            "kernel": "ef_kernel<df, float> (fused 1p basis, A, AA trie energy + adjoint, forces)",
             "peak_source": "measured in this run: cuBLAS SGEMM 8192^3, TF32 off (CUDA-core FP32)",
             "flops_per_env": fl / nenv}
     cpu = None if args.no_cpu else cpu_baseline(spec, c, b)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "vs_baseline": None, "dtype": "f32x2", "data": "synthetic (seeded)",
             "config": {"workload": WORKLOAD["name"], "nenv_per_gpu": nenv, "nnbr_per_gpu": nnbr,
-                       "form": "fp32 (Rn/Ylm/A/AA/adjoint in FP32, energy block sums in FP64)",
+                       "form": "fp32x2: Rn, Ylm, A and the AA energy in double-float (FP32 pairs), adjoint and forces in FP32",
                        "l2": "flushed (256 MB write) between timed steps", "parallelism": f"replicas x{world}"},
             "forms": {"fp64": {"value": nenv * k64 * world / t64, "ms_per_step": 1e3 * t64 / k64},
-                      "fp32": {"value": value, "ms_per_step": ms}},
+                      "fp32": {"value": nenv * args.steps * world / t32p, "ms_per_step": 1e3 * t32p / args.steps,
+                               "error": err32},
+                      "fp32x2": {"value": value, "ms_per_step": ms, "error": err}},
             "error": err, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
             "gpu_launches": int(launches), "peaks_measured": peaks}
     print(json.dumps(line), flush=True)
