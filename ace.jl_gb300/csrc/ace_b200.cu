@@ -177,25 +177,28 @@ extern "C" int ace_ctx_create(const ace_spec_bundle *s, int32_t prec, int32_t de
   {
     Schedule sch = build_schedule(s->nA, s->a_n, s->a_l, s->a_m, s->a_mu, s->nAA, s->maxord, s->orders,
                                   s->iAA2iA, s->nB, s->U_indptr, s->U_indices, s->U_data, ctx->nt);
+    Interleaved il = interleave(sch, ctx->nt);
     ctx->sn = sch.n;
     ctx->halved = sch.halved;
     ctx->sched_nodes = sch.nodes;
-    ctx->sk = sch.k;
-    ctx->sw = sch.w;
-    if ((rc = upload(ctx, &ctx->d_sv, sch.v.data(), sch.v.size())) ||
-        (rc = upload(ctx, &ctx->d_sord, sch.ord.data(), sch.ord.size())) ||
-        (rc = upload(ctx, &ctx->d_sq, sch.q.data(), sch.q.size())) ||
-        (rc = upload(ctx, &ctx->d_sstart, sch.start.data(), sch.start.size()))) {
+    ctx->slen = il.len;
+    const int64_t nslot = std::max<int64_t>(il.len * ctx->nt, 1);
+    ctx->sslot.assign(nslot, -1);
+    ctx->sw.assign(nslot, 0);
+    for (int64_t j = 0; j < il.len * ctx->nt; ++j)
+      if (il.perm[j] >= 0) { ctx->sslot[j] = sch.k[il.perm[j]]; ctx->sw[j] = sch.w[il.perm[j]]; }
+    if (il.rec.empty()) il.rec.assign(8, 0);
+    if ((rc = upload(ctx, (uint16_t **)&ctx->d_srec, il.rec.data(), il.rec.size()))) {
       g_create_error = ctx->err;
       return fail(rc);
     }
     const size_t csz = (prec == ACE_PREC_FP64) ? 8 : (prec == ACE_PREC_FP32X2 ? 8 : 4);
-    if (cudaMalloc(&ctx->d_sc, std::max<int64_t>(sch.n, 1) * csz) != cudaSuccess) {
+    if (cudaMalloc(&ctx->d_sc, nslot * csz) != cudaSuccess) {
       g_create_error = "cudaMalloc failed";
       return fail(ACE_ERR_ALLOC);
     }
     ctx->allocs.push_back(ctx->d_sc);
-    cudaMemset(ctx->d_sc, 0, std::max<int64_t>(sch.n, 1) * csz);
+    cudaMemset(ctx->d_sc, 0, nslot * csz);
   }
   // U (host copy for c~ = U^T c; device copy for the basis path)
   if (s->nB > 0) {
@@ -246,26 +249,25 @@ extern "C" int ace_ctx_destroy(ace_ctx *ctx) {
 // Pack w * c~ in schedule order, in the energy type of the precision mode.
 static int push_ctilde(ace_ctx *ctx) {
   ACE_CUDA(cudaSetDevice(ctx->device));
-  const int64_t n = ctx->sn;
-  if (n > 0) {
-    if (ctx->prec == ACE_PREC_FP64) {
-      std::vector<double> c(n);
-      for (int64_t i = 0; i < n; ++i) c[i] = ctx->sw[i] * ctx->ctilde[ctx->sk[i]];
-      ACE_CUDA(cudaMemcpy(ctx->d_sc, c.data(), n * 8, cudaMemcpyHostToDevice));
-    } else if (ctx->prec == ACE_PREC_FP32X2) {
-      std::vector<float> c(2 * n);
-      for (int64_t i = 0; i < n; ++i) {
-        const double v = ctx->sw[i] * ctx->ctilde[ctx->sk[i]];
-        const float h = (float)v;
-        c[2 * i] = h;
-        c[2 * i + 1] = (float)(v - (double)h);
-      }
-      ACE_CUDA(cudaMemcpy(ctx->d_sc, c.data(), n * 8, cudaMemcpyHostToDevice));
-    } else {
-      std::vector<float> c(n);
-      for (int64_t i = 0; i < n; ++i) c[i] = (float)(ctx->sw[i] * ctx->ctilde[ctx->sk[i]]);
-      ACE_CUDA(cudaMemcpy(ctx->d_sc, c.data(), n * 4, cudaMemcpyHostToDevice));
+  const int64_t n = (int64_t)ctx->sslot.size();
+  auto val = [&](int64_t j) { return ctx->sslot[j] < 0 ? 0.0 : ctx->sw[j] * ctx->ctilde[ctx->sslot[j]]; };
+  if (ctx->prec == ACE_PREC_FP64) {
+    std::vector<double> c(n);
+    for (int64_t j = 0; j < n; ++j) c[j] = val(j);
+    ACE_CUDA(cudaMemcpy(ctx->d_sc, c.data(), n * 8, cudaMemcpyHostToDevice));
+  } else if (ctx->prec == ACE_PREC_FP32X2) {
+    std::vector<float> c(2 * n);
+    for (int64_t j = 0; j < n; ++j) {
+      const double v = val(j);
+      const float h = (float)v;
+      c[2 * j] = h;
+      c[2 * j + 1] = (float)(v - (double)h);
     }
+    ACE_CUDA(cudaMemcpy(ctx->d_sc, c.data(), n * 8, cudaMemcpyHostToDevice));
+  } else {
+    std::vector<float> c(n);
+    for (int64_t j = 0; j < n; ++j) c[j] = (float)val(j);
+    ACE_CUDA(cudaMemcpy(ctx->d_sc, c.data(), n * 4, cudaMemcpyHostToDevice));
   }
   return ACE_OK;
 }

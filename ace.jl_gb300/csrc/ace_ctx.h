@@ -42,12 +42,11 @@ struct ace_ctx {
   int64_t sn = 0;
   bool halved = false;
   int64_t sched_nodes = 0;
-  uint16_t *d_sv = nullptr;
-  uint8_t *d_sord = nullptr, *d_sq = nullptr;
-  int32_t *d_sstart = nullptr;
-  void *d_sc = nullptr;        // packed coefficients in the energy type
-  std::vector<int32_t> sk;     // schedule -> AA index
-  std::vector<uint8_t> sw;     // weights
+  int64_t slen = 0;            // interleaved slots per thread
+  uint4 *d_srec = nullptr;     // [slen * nt] packed records (ace_sched.h)
+  void *d_sc = nullptr;        // [slen * nt] coefficients w * c~ in the energy type
+  std::vector<int64_t> sslot;  // slot -> AA index (-1: empty slot)
+  std::vector<uint8_t> sw;     // slot -> weight
 
   // host copies
   std::vector<double> ctilde;

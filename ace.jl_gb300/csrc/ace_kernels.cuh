@@ -46,12 +46,10 @@ struct EFArgs {
   int ntab, nR, L, pl, pr, tp;
   const int16_t *an, *aiy, *amu;
   int nA, nspecies;
-  // correlation schedule
-  const uint16_t *sv;
-  const uint8_t *sord, *sq;
+  // correlation schedule: interleaved records and coefficients (ace_sched.h)
+  const uint4 *srec;
   const void *sc;
-  int64_t sn;
-  const int32_t *sstart;
+  int64_t slen;
   double c0;
   int chunkE, chunkG, npriv;
   int *status;
@@ -81,14 +79,18 @@ inline __host__ __device__ EFLayout ef_layout(int ntab, int nR, int L, int nA, i
   l.AE = o; o = al16(o + (size_t)nA * 2 * sE);
   l.AG = same ? l.AE : o; if (!same) o = al16(o + (size_t)nA * 2 * sG);
   l.D = o; o = al16(o + (size_t)nA * 2 * sG);
-  l.priv = o; o = al16(o + (size_t)npriv * nt * 2 * sG);
   const int ch = chunkE > chunkG ? chunkE : chunkG;
   l.pos = o; o = al16(o + (size_t)ch * 4 * sG);
   l.spc = o; o = al16(o + (size_t)ch * 4);
   l.slabE = nR + szP + 2 * nY;
   l.slabG = 2 * nR + 2 * szP + 8 * nY;
+  // the neighbour slabs (phases 1, 3) and the private adjoint bins (phase 2)
+  // are never live at the same time and share one region
   const size_t bE = (size_t)chunkE * l.slabE * sE, bG = (size_t)chunkG * l.slabG * sG;
-  l.slab = o; o = al16(o + (bE > bG ? bE : bG));
+  const size_t bP = (size_t)npriv * nt * 2 * sG;
+  size_t big = bE > bG ? bE : bG;
+  big = big > bP ? big : bP;
+  l.slab = o; l.priv = o; o = al16(o + big);
   l.red = o; o = al16(o + 32 * 8);
   l.total = o;
   return l;
@@ -197,15 +199,12 @@ __global__ void __launch_bounds__(NT) ef_kernel(EFArgs a) {
     if (!SAME) tabG[i] = load_table<TG>(a.tabG, i);
   }
   for (int i = tid; i < a.nA; i += NT) { s_an[i] = a.an[i]; s_aiy[i] = a.aiy[i]; s_amu[i] = a.amu[i]; }
-  if (GRAD)
-    for (int i = tid; i < npriv * NT; i += NT) priv[i] = {TG(0), TG(0)};
   __syncthreads();
   Tables<TE> tbE;
   tbE.bind(tabE, a.nR, a.L, a.pl, a.pr, a.tp);
   Tables<TG> tbG;
   tbG.bind(tabG, a.nR, a.L, a.pl, a.pr, a.tp);
   const int64_t ntot = a.off[a.nEnv];
-  const int r0 = a.sstart[tid], r1 = a.sstart[tid + 1];
 
   for (int64_t e = blockIdx.x; e < a.nEnv; e += gridDim.x) {
     const int64_t o0 = a.off[e], o1 = a.off[e + 1];
@@ -224,6 +223,7 @@ __global__ void __launch_bounds__(NT) ef_kernel(EFArgs a) {
         if (!SAME) AG[i] = {lower<TG>(AE[i].re), lower<TG>(AE[i].im)};
         D[i] = {TG(0), TG(0)};
       }
+      for (int i = tid; i < npriv * NT; i += NT) priv[i] = {TG(0), TG(0)};
       __syncthreads();
     }
     // ---------------- phase 2
@@ -257,16 +257,20 @@ __global__ void __launch_bounds__(NT) ef_kernel(EFArgs a) {
         H[d - 1] = cadd(H[d - 1], cmul(Ac[d], H[d]));
       }
     };
-    for (int i = r0; i < r1; ++i) {
-      const int q = a.sq[i], k = a.sord[i];
-      const TE c = load_coef<TE>(a.sc, i);
+    for (int64_t j = 0; j < a.slen; ++j) {
+      const int64_t slot = j * NT + tid;
+      const uint4 rc = a.srec[slot];
+      const int k = rc.w & 0xff, q = (rc.w >> 8) & 0xff;
+      if (k == 0) continue;
+      const TE c = load_coef<TE>(a.sc, slot);
+      const uint32_t vw[3] = {rc.x, rc.y, rc.z};
 #pragma unroll
       for (int d = K; d >= 1; --d)
         if (d <= cur && d > q) close(d);
 #pragma unroll
       for (int d = 1; d <= K; ++d) {
         if (d > q && d <= k) {
-          const int u = a.sv[(size_t)(d - 1) * a.sn + i];
+          const int u = (vw[(d - 1) >> 1] >> (16 * ((d - 1) & 1))) & 0xffff;
           vc[d] = u;
           Ac[d] = AE[u];
           if (GRAD && d < K) bar[d] = cmul(bar[d - 1], AG[u]);
@@ -290,9 +294,8 @@ __global__ void __launch_bounds__(NT) ef_kernel(EFArgs a) {
       for (int u = w; u < npriv; u += NT / 32) {
         TG sr = TG(0), si = TG(0);
         for (int t = lane; t < NT; t += 32) {
-          cpx<TG> *p = priv + u * NT + t;
+          const cpx<TG> *p = priv + u * NT + t;
           sr += p->re; si += p->im;
-          *p = {TG(0), TG(0)};
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
@@ -301,6 +304,7 @@ __global__ void __launch_bounds__(NT) ef_kernel(EFArgs a) {
         }
         if (lane == 0 && u < a.nA) { D[u].re += sr; D[u].im += si; }
       }
+      __syncthreads();
     }
     // ---------------- phase 3: forces
     const int lane = tid & 31, w = tid >> 5, nw = NT >> 5;

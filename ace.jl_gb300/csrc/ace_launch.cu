@@ -52,12 +52,14 @@ int kernels_prepare(ace_ctx *ctx) {
   bool same;
   type_sizes(ctx, sE, sG, same);
   ctx->nt = NT;
-  // neighbour chunks of ~32 KB slabs each; private adjoint bins in ~32 KB
+  // one ~40 KB region holds the neighbour slabs (phases 1, 3) or the private
+  // adjoint bins (phase 2)
+  const int region = 40 * 1024;
   const int slabE = (ctx->nR + size_p(ctx->L) + 2 * size_y(ctx->L)) * sE;
   const int slabG = (2 * ctx->nR + 2 * size_p(ctx->L) + 8 * size_y(ctx->L)) * sG;
-  ctx->chunkE = std::max(1, std::min(64, (32 * 1024) / slabE));
-  ctx->chunkG = std::max(1, std::min(32, (32 * 1024) / slabG));
-  ctx->npriv = std::max(1, std::min(ctx->nA, (32 * 1024) / (NT * 2 * sG)));
+  ctx->chunkE = std::max(1, std::min(64, region / slabE));
+  ctx->chunkG = std::max(1, std::min(32, region / slabG));
+  ctx->npriv = std::max(1, std::min(ctx->nA, region / (NT * 2 * sG)));
   EFLayout lay = ef_layout(ctx->ntab, ctx->nR, ctx->L, ctx->nA, ctx->chunkE, ctx->chunkG, ctx->npriv, NT, sE, sG, same);
   while (lay.total > (size_t)ctx->smem_optin && (ctx->chunkE > 1 || ctx->chunkG > 1 || ctx->npriv > 1)) {
     ctx->chunkE = std::max(1, ctx->chunkE / 2);
@@ -107,8 +109,7 @@ static EFArgs make_args(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const do
   a.ntab = ctx->ntab; a.nR = ctx->nR; a.L = ctx->L; a.pl = ctx->pl; a.pr = ctx->pr; a.tp = ctx->tp;
   a.an = ctx->d_an; a.aiy = ctx->d_aiy; a.amu = ctx->d_amu;
   a.nA = ctx->nA; a.nspecies = ctx->nspecies;
-  a.sv = ctx->d_sv; a.sord = ctx->d_sord; a.sq = ctx->d_sq; a.sc = ctx->d_sc; a.sn = ctx->sn;
-  a.sstart = ctx->d_sstart;
+  a.srec = ctx->d_srec; a.sc = ctx->d_sc; a.slen = ctx->slen;
   a.c0 = ctx->has_const ? ctx->ctilde[0] : 0.0;
   a.chunkE = ctx->chunkE; a.chunkG = ctx->chunkG; a.npriv = ctx->npriv;
   a.status = ctx->d_status;

@@ -124,21 +124,42 @@ inline Schedule build_schedule(int nA, const int32_t *a_n, const int32_t *a_l, c
     s.q[i] = (uint8_t)qq;
     cost[i] = 1.0 + 2.0 * (double)(t.size() - qq);
   }
-  // ---- balanced contiguous ranges
+  // ---- contiguous ranges of (nearly) equal length, one per thread
   s.start.assign(nthreads + 1, 0);
-  const double total = std::accumulate(cost.begin(), cost.end(), 0.0);
-  double acc = 0.0;
-  int th = 1;
-  for (int64_t i = 0; i < s.n && th < nthreads; ++i) {
-    acc += cost[i];
-    while (th < nthreads && acc >= total * th / nthreads) s.start[th++] = (int32_t)(i + 1);
-  }
-  while (th <= nthreads) s.start[th++] = (int32_t)s.n;
+  for (int t = 0; t <= nthreads; ++t) s.start[t] = (int32_t)((s.n * (int64_t)t) / nthreads);
   // a range starts from an empty path
   for (int t = 0; t < nthreads; ++t)
     if (s.start[t] < s.n) s.q[s.start[t]] = 0;
   for (int64_t i = 0; i < s.n; ++i) s.nodes += s.ord[i] - s.q[i];
   return s;
+}
+
+// Thread-interleaved records: slot (j * nthreads + t) holds the j-th function
+// of thread t's range, so that the lanes of a warp read adjacent 16-byte
+// records.  Record: v[0..5] (uint16), ord (uint8), q (uint8), 2 bytes pad;
+// ord == 0 marks an empty slot.  perm[slot] is the schedule index (-1: empty).
+struct Interleaved {
+  int64_t len = 0;                 // slots per thread
+  std::vector<uint16_t> rec;       // [len * nthreads * 8]
+  std::vector<int64_t> perm;       // [len * nthreads]
+};
+
+inline Interleaved interleave(const Schedule &s, int nthreads) {
+  Interleaved r;
+  int64_t mx = 0;
+  for (int t = 0; t < nthreads; ++t) mx = std::max<int64_t>(mx, s.start[t + 1] - s.start[t]);
+  r.len = mx;
+  r.rec.assign((size_t)mx * nthreads * 8, 0);
+  r.perm.assign((size_t)mx * nthreads, -1);
+  for (int t = 0; t < nthreads; ++t)
+    for (int64_t i = s.start[t], j = 0; i < s.start[t + 1]; ++i, ++j) {
+      const size_t slot = (size_t)j * nthreads + t;
+      uint16_t *rc = &r.rec[8 * slot];
+      for (int d = 0; d < s.K && d < 6; ++d) rc[d] = s.v[(size_t)d * s.n + i];
+      rc[6] = (uint16_t)(s.ord[i] | (s.q[i] << 8));
+      r.perm[slot] = i;
+    }
+  return r;
 }
 
 }  // namespace ace
