@@ -23,7 +23,7 @@ ACE_ASYNC = 4
 
 EXPORTED = ("ace_ctx_create", "ace_ctx_destroy", "ace_set_params", "ace_set_ctilde",
             "ace_energy_forces", "ace_energy", "ace_basis", "ace_sync", "ace_get_spec_sizes",
-            "ace_last_error_string", "ace_launch_count")
+            "ace_last_error_string", "ace_launch_count", "ace_basis_noalloc")
 
 
 class AceError(RuntimeError):
@@ -66,6 +66,7 @@ def load(path: str | None = None):
     lib.ace_energy_forces.argtypes = [P, C.c_int64, P, P, P, P, P, C.c_int32, P]
     lib.ace_energy.argtypes = [P, C.c_int64, P, P, P, P, C.c_int32, P]
     lib.ace_basis.argtypes = [P, C.c_int64, P, P, P, P, P, C.c_int32, P]
+    lib.ace_basis_noalloc.argtypes = [P, C.c_int64, P, P, P, P, P]
     lib.ace_sync.argtypes = [P]
     lib.ace_get_spec_sizes.argtypes = [P, P]
     lib.ace_last_error_string.argtypes = [P]
@@ -73,7 +74,8 @@ def load(path: str | None = None):
     lib.ace_launch_count.argtypes = [P]
     lib.ace_launch_count.restype = C.c_int64
     for name in ("ace_ctx_create", "ace_ctx_destroy", "ace_set_params", "ace_set_ctilde",
-                 "ace_energy_forces", "ace_energy", "ace_basis", "ace_sync", "ace_get_spec_sizes"):
+                 "ace_energy_forces", "ace_energy", "ace_basis", "ace_sync", "ace_get_spec_sizes",
+                 "ace_basis_noalloc"):
         getattr(lib, name).restype = C.c_int
     _lib = lib
     return lib

@@ -417,4 +417,25 @@ __global__ void ub_kernel(int64_t ne, int64_t e0, int64_t ldE, int64_t nB, const
   }
 }
 
+// Kernel arguments for a context (host side).
+inline EFArgs make_args(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const double *rr, const int32_t *sp,
+                        double *E, double *G) {
+  EFArgs a{};
+  a.nEnv = nEnv; a.off = off; a.rr = rr; a.sp = sp; a.E = E; a.G = G;
+  switch (ctx->prec) {
+    case ACE_PREC_FP64: a.tabE = ctx->d_tabD; a.tabG = ctx->d_tabD; break;
+    case ACE_PREC_FP32X2: a.tabE = ctx->d_tabDF; a.tabG = ctx->d_tabF; break;
+    default: a.tabE = ctx->d_tabF; a.tabG = ctx->d_tabF; break;
+  }
+  a.ntab = ctx->ntab; a.nR = ctx->nR; a.L = ctx->L; a.pl = ctx->pl; a.pr = ctx->pr; a.tp = ctx->tp;
+  a.an = ctx->d_an; a.aiy = ctx->d_aiy; a.amu = ctx->d_amu;
+  a.nA = ctx->nA; a.nspecies = ctx->nspecies;
+  a.srec = ctx->d_srec; a.sc = ctx->d_sc; a.slen = ctx->slen;
+  a.c0 = ctx->has_const ? ctx->ctilde[0] : 0.0;
+  a.chunkE = ctx->chunkE; a.chunkG = ctx->chunkG; a.npriv = ctx->npriv;
+  a.status = ctx->d_status;
+  a.ord = ctx->d_ord; a.idx = ctx->d_idx; a.nAA = ctx->nAA;
+  return a;
+}
+
 }  // namespace ace

@@ -132,6 +132,21 @@ int ace_energy(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, const double 
 int ace_basis(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, const double *rr,
               const int32_t *species, double *B, double *dB, int32_t flags, void *stream);
 
+/* The symmetric basis B (as ace_basis, without dB) for callers that must not
+   allocate device memory while they run -- e.g. an MD engine that owns the
+   device memory pool after start-up, or a service with a fixed footprint.
+   No counterpart in the reference (ACE.jl allocates per call).  Allocates
+   nothing: inputs and B must be device pointers; its scratch is a 16 MiB
+   static device array held by every GPU that loads the library.  Specs whose
+   per-environment AA vector (nAA x 8 bytes, or x 4 in FP32 mode) exceeds
+   16 MiB are rejected with ACE_ERR_UNSUPPORTED.  The first call on a device
+   looks up the array's device address; make that first call before any
+   stream capture.  Runs asynchronously on `stream` (ace_sync reports the
+   kernels' status).  All calls share the scratch: calls that overlap on the
+   GPU race and must be serialised by the caller. */
+int ace_basis_noalloc(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, const double *rr,
+                      const int32_t *species, double *B, void *stream);
+
 /* Wait for the context's outstanding work; returns the kernels' status. */
 int ace_sync(ace_ctx *ctx);
 
