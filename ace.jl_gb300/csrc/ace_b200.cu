@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -193,6 +194,31 @@ extern "C" int ace_ctx_create(const ace_spec_bundle *s, int32_t prec, int32_t de
       return fail(rc);
     }
     const size_t csz = (prec == ACE_PREC_FP64) ? 8 : (prec == ACE_PREC_FP32X2 ? 8 : 4);
+    // item schedule
+    const char *kenv = getenv("ACE_B200_KERNEL");
+    ctx->use_items = !(kenv && std::string(kenv) == "trie");
+    ItemSchedule its = build_items(sch, ctx->nt);
+    ctx->item_n = its.n;
+    ctx->ik.assign((size_t)(ITEM_G + 1) * its.n, -1);
+    ctx->iw.assign((size_t)(ITEM_G + 1) * its.n, 0);
+    for (int64_t f = 0; f < its.n; ++f) {
+      ctx->ik[f] = its.kown[f];
+      ctx->iw[f] = its.wown[f];
+      for (int g = 0; g < ITEM_G; ++g) {
+        ctx->ik[(size_t)(g + 1) * its.n + f] = its.kleaf[(size_t)f * ITEM_G + g];
+        ctx->iw[(size_t)(g + 1) * its.n + f] = its.wleaf[(size_t)f * ITEM_G + g];
+      }
+    }
+    if ((rc = upload(ctx, (uint16_t **)&ctx->d_irec, its.rec.data(), its.rec.size()))) {
+      g_create_error = ctx->err;
+      return fail(rc);
+    }
+    if (cudaMalloc(&ctx->d_ic, ctx->ik.size() * csz) != cudaSuccess) {
+      g_create_error = "cudaMalloc failed";
+      return fail(ACE_ERR_ALLOC);
+    }
+    ctx->allocs.push_back(ctx->d_ic);
+    cudaMemset(ctx->d_ic, 0, ctx->ik.size() * csz);
     if (cudaMalloc(&ctx->d_sc, nslot * csz) != cudaSuccess) {
       g_create_error = "cudaMalloc failed";
       return fail(ACE_ERR_ALLOC);
@@ -247,8 +273,34 @@ extern "C" int ace_ctx_destroy(ace_ctx *ctx) {
 }
 
 // Pack w * c~ in schedule order, in the energy type of the precision mode.
+static int pack_coefs(ace_ctx *ctx, void *dst, int64_t n, const std::function<double(int64_t)> &val) {
+  if (ctx->prec == ACE_PREC_FP64) {
+    std::vector<double> c(n);
+    for (int64_t j = 0; j < n; ++j) c[j] = val(j);
+    ACE_CUDA(cudaMemcpy(dst, c.data(), n * 8, cudaMemcpyHostToDevice));
+  } else if (ctx->prec == ACE_PREC_FP32X2) {
+    std::vector<float> c(2 * n);
+    for (int64_t j = 0; j < n; ++j) {
+      const double v = val(j);
+      const float h = (float)v;
+      c[2 * j] = h;
+      c[2 * j + 1] = (float)(v - (double)h);
+    }
+    ACE_CUDA(cudaMemcpy(dst, c.data(), n * 8, cudaMemcpyHostToDevice));
+  } else {
+    std::vector<float> c(n);
+    for (int64_t j = 0; j < n; ++j) c[j] = (float)val(j);
+    ACE_CUDA(cudaMemcpy(dst, c.data(), n * 4, cudaMemcpyHostToDevice));
+  }
+  return ACE_OK;
+}
+
 static int push_ctilde(ace_ctx *ctx) {
   ACE_CUDA(cudaSetDevice(ctx->device));
+  int rc = pack_coefs(ctx, ctx->d_ic, (int64_t)ctx->ik.size(), [&](int64_t j) {
+    return ctx->ik[j] < 0 ? 0.0 : ctx->iw[j] * ctx->ctilde[ctx->ik[j]];
+  });
+  if (rc) return rc;
   const int64_t n = (int64_t)ctx->sslot.size();
   auto val = [&](int64_t j) { return ctx->sslot[j] < 0 ? 0.0 : ctx->sw[j] * ctx->ctilde[ctx->sslot[j]]; };
   if (ctx->prec == ACE_PREC_FP64) {

@@ -47,6 +47,13 @@ struct ace_ctx {
   void *d_sc = nullptr;        // [slen * nt] coefficients w * c~ in the energy type
   std::vector<int64_t> sslot;  // slot -> AA index (-1: empty slot)
   std::vector<uint8_t> sw;     // slot -> weight
+  // item schedule (ace_sched.h build_items)
+  bool use_items = true;
+  int64_t item_n = 0;
+  uint4 *d_irec = nullptr;
+  void *d_ic = nullptr;        // [(G+1) * item_n] coefficients in the energy type
+  std::vector<int64_t> ik;     // [(G+1) * item_n] AA index (-1: none)
+  std::vector<uint8_t> iw;     // weights
 
   // host copies
   std::vector<double> ctilde;

@@ -30,6 +30,7 @@
 #include "ace_arith.cuh"
 #include "ace_ctx.h"
 #include "ace_phi.cuh"
+#include "ace_sched.h"
 
 namespace ace {
 
@@ -50,6 +51,10 @@ struct EFArgs {
   const uint4 *srec;
   const void *sc;
   int64_t slen;
+  // item schedule (ace_sched.h): records and (G+1) coefficient rows
+  const uint4 *irec;
+  const void *ic;
+  int64_t in;
   double c0;
   int chunkE, chunkG, npriv;
   int *status;
@@ -172,7 +177,13 @@ __device__ __forceinline__ void build_A(const EFArgs &a, const Tables<T> &tb, in
   __syncthreads();
 }
 
-template <typename TE, typename TG, int K, int NT, bool GRAD>
+template <typename T> __device__ __forceinline__ cpx<T> shfl_down_c(cpx<T> v, int off) {
+  return {__shfl_down_sync(0xffffffffu, v.re, off), __shfl_down_sync(0xffffffffu, v.im, off)};
+}
+
+// ITEMS selects the phase-2 algorithm: false = per-thread trie walk over the
+// lexicographic schedule, true = uniform items (ace_sched.h build_items).
+template <typename TE, typename TG, int K, int NT, bool GRAD, bool ITEMS>
 __global__ void __launch_bounds__(NT) ef_kernel(EFArgs a) {
   constexpr bool SAME = std::is_same<TE, TG>::value;
   extern __shared__ __align__(16) unsigned char sm[];
@@ -227,6 +238,18 @@ __global__ void __launch_bounds__(NT) ef_kernel(EFArgs a) {
       __syncthreads();
     }
     // ---------------- phase 2
+    auto dacc = [&](int u, cpx<TG> v) {
+      if (u < npriv) {
+        cpx<TG> *p = priv + u * NT + tid;
+        p->re += v.re;
+        p->im += v.im;
+      } else {
+        atomicAdd(&D[u].re, v.re);
+        atomicAdd(&D[u].im, v.im);
+      }
+    };
+    TE eacc = Arith<TE>::zero();
+    if constexpr (!ITEMS) {
     cpx<TE> H[K + 1], Ac[K + 1];
     cpx<TG> bar[K + 1];
     int vc[K + 1];
@@ -238,16 +261,6 @@ __global__ void __launch_bounds__(NT) ef_kernel(EFArgs a) {
       vc[d] = 0;
     }
     int cur = 0;
-    auto dacc = [&](int u, cpx<TG> v) {
-      if (u < npriv) {
-        cpx<TG> *p = priv + u * NT + tid;
-        p->re += v.re;
-        p->im += v.im;
-      } else {
-        atomicAdd(&D[u].re, v.re);
-        atomicAdd(&D[u].im, v.im);
-      }
-    };
     auto close = [&](int d) {
       if (d == K) {  // leaf: H_K is the (real) coefficient
         if (GRAD) dacc(vc[K], cscale(bar[K - 1], lower<TG>(H[K].re)));
@@ -285,7 +298,73 @@ __global__ void __launch_bounds__(NT) ef_kernel(EFArgs a) {
 #pragma unroll
     for (int d = K; d >= 1; --d)
       if (d <= cur) close(d);
-    const double esum = block_sum(lower<double>(H[0].re), red);
+      eacc = H[0].re;
+    } else {
+      constexpr int KP = (K > 1) ? K - 1 : 1;
+      const int lane = tid & 31;
+      const cpx<TG> gone = {TG(1), TG(0)};
+      for (int64_t f = tid; f < a.in; f += NT) {
+        const uint4 rc = a.irec[f];
+        const int P = (rc.w >> 16) & 0xf, nl = (rc.w >> 20) & 0xf;
+        const unsigned heads = (rc.w >> 24) & 0xff;
+        const uint32_t vw[4] = {rc.x, rc.y, rc.z, rc.w};
+        cpx<TE> bar = {Arith<TE>::one(), Arith<TE>::zero()};
+        cpx<TG> aG[KP];
+        int vi[KP];
+#pragma unroll
+        for (int d = 0; d < KP; ++d) {
+          vi[d] = (int)((vw[d >> 1] >> (16 * (d & 1))) & 0xffff);
+          aG[d] = gone;
+          if (d < P) {
+            const cpx<TE> ae = AE[vi[d]];
+            bar = (d == 0) ? ae : cmul(bar, ae);
+            if (GRAD) aG[d] = AG[vi[d]];
+          }
+        }
+        cpx<TE> H = {load_coef<TE>(a.ic, f), Arith<TE>::zero()};
+        TE cl[ITEM_G];
+        int ul[ITEM_G];
+#pragma unroll
+        for (int g = 0; g < ITEM_G; ++g) {
+          ul[g] = (int)((vw[(5 + g) >> 1] >> (16 * ((5 + g) & 1))) & 0xffff);
+          cl[g] = load_coef<TE>(a.ic, (int64_t)(g + 1) * a.in + f);
+          if (g < nl) H = cadd(H, cscale(AE[ul[g]], cl[g]));
+        }
+        if (P > 0) eacc = eacc + (bar.re * H.re - bar.im * H.im);
+        if (GRAD) {
+          cpx<TG> pre[KP], suf[KP];
+          pre[0] = gone;
+#pragma unroll
+          for (int d = 1; d < KP; ++d) pre[d] = (d < P) ? cmul(pre[d - 1], aG[d - 1]) : pre[d - 1];
+          suf[KP - 1] = gone;
+#pragma unroll
+          for (int d = KP - 2; d >= 0; --d) suf[d] = (d + 1 < P) ? cmul(aG[d + 1], suf[d + 1]) : gone;
+          const cpx<TG> bG = cmul(pre[KP - 1], aG[KP - 1]);
+          const cpx<TG> h = {lower<TG>(H.re), lower<TG>(H.im)};
+#pragma unroll
+          for (int g = 0; g < ITEM_G; ++g)
+            if (g < nl) dacc(ul[g], cscale(bG, lower<TG>(cl[g])));
+#pragma unroll
+          for (int d = 0; d < KP; ++d) {
+            cpx<TG> v = (d < P) ? cmul(cmul(pre[d], suf[d]), h) : cpx<TG>{TG(0), TG(0)};
+            if (d < KP - 1) {
+              // runs of equal (v1..v_{d+1}) are adjacent lanes: reduce into each run's head
+              const unsigned hm = __ballot_sync(0xffffffffu, (heads >> d) & 1u);
+#pragma unroll
+              for (int off = 1; off < 32; off <<= 1) {
+                const cpx<TG> o = shfl_down_c(v, off);
+                const unsigned between = (unsigned)(((unsigned long long)hm >> (lane + 1)) & ((1ull << off) - 1ull));
+                if (lane + off < 32 && between == 0u) { v.re += o.re; v.im += o.im; }
+              }
+              if (((heads >> d) & 1u) && d < P) dacc(vi[d], v);
+            } else if (d < P) {
+              dacc(vi[d], v);
+            }
+          }
+        }
+      }
+    }
+    const double esum = block_sum(lower<double>(eacc), red);
     if (tid == 0) a.E[e] = a.c0 + esum;
     if (!GRAD) continue;
     // private bins -> D (one warp per bin, lanes over threads)
@@ -431,6 +510,7 @@ inline EFArgs make_args(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const do
   a.an = ctx->d_an; a.aiy = ctx->d_aiy; a.amu = ctx->d_amu;
   a.nA = ctx->nA; a.nspecies = ctx->nspecies;
   a.srec = ctx->d_srec; a.sc = ctx->d_sc; a.slen = ctx->slen;
+  a.irec = ctx->d_irec; a.ic = ctx->d_ic; a.in = ctx->item_n;
   a.c0 = ctx->has_const ? ctx->ctilde[0] : 0.0;
   a.chunkE = ctx->chunkE; a.chunkG = ctx->chunkG; a.npriv = ctx->npriv;
   a.status = ctx->d_status;

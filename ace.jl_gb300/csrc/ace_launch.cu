@@ -11,23 +11,29 @@ namespace ace {
 
 static constexpr int NT = 128;  // threads per CTA of the energy/forces kernel
 
-template <typename TE, typename TG, bool GRAD>
+template <typename TE, typename TG, bool GRAD, bool ITEMS>
 static void *ef_func_k(int K) {
   switch (K) {
     case 1:
-    case 2: return (void *)ef_kernel<TE, TG, 2, NT, GRAD>;
-    case 3: return (void *)ef_kernel<TE, TG, 3, NT, GRAD>;
-    case 4: return (void *)ef_kernel<TE, TG, 4, NT, GRAD>;
-    case 5: return (void *)ef_kernel<TE, TG, 5, NT, GRAD>;
-    default: return (void *)ef_kernel<TE, TG, 6, NT, GRAD>;
+    case 2: return (void *)ef_kernel<TE, TG, 2, NT, GRAD, ITEMS>;
+    case 3: return (void *)ef_kernel<TE, TG, 3, NT, GRAD, ITEMS>;
+    case 4: return (void *)ef_kernel<TE, TG, 4, NT, GRAD, ITEMS>;
+    case 5: return (void *)ef_kernel<TE, TG, 5, NT, GRAD, ITEMS>;
+    default: return (void *)ef_kernel<TE, TG, 6, NT, GRAD, ITEMS>;
   }
+}
+
+template <typename TE, typename TG>
+static void *ef_func_t(const ace_ctx *ctx, bool grad) {
+  if (ctx->use_items) return grad ? ef_func_k<TE, TG, true, true>(ctx->maxord) : ef_func_k<TE, TG, false, true>(ctx->maxord);
+  return grad ? ef_func_k<TE, TG, true, false>(ctx->maxord) : ef_func_k<TE, TG, false, false>(ctx->maxord);
 }
 
 static void *ef_func(const ace_ctx *ctx, bool grad) {
   switch (ctx->prec) {
-    case ACE_PREC_FP64: return grad ? ef_func_k<double, double, true>(ctx->maxord) : ef_func_k<double, double, false>(ctx->maxord);
-    case ACE_PREC_FP32X2: return grad ? ef_func_k<df, float, true>(ctx->maxord) : ef_func_k<df, float, false>(ctx->maxord);
-    default: return grad ? ef_func_k<float, float, true>(ctx->maxord) : ef_func_k<float, float, false>(ctx->maxord);
+    case ACE_PREC_FP64: return ef_func_t<double, double>(ctx, grad);
+    case ACE_PREC_FP32X2: return ef_func_t<df, float>(ctx, grad);
+    default: return ef_func_t<float, float>(ctx, grad);
   }
 }
 

@@ -162,4 +162,100 @@ inline Interleaved interleave(const Schedule &s, int nthreads) {
   return r;
 }
 
+// ----------------------------------------------------------------------------
+// Item schedule (uniform per-lane work).  A depth-(K-1) prefix p = (v1..v_{K-1})
+// together with up to G of its leaves (v1..v_{K-1}, u) is one item; a prefix
+// with more leaves is split into several items (every quantity an item
+// contributes is linear in its leaves, so the split is exact).  The
+// coefficient of the prefix function itself, if p is a function, rides on
+// the prefix's first item.  Functions of order < K-1 are items with no
+// leaves.  Items are sorted lexicographically by prefix (full-length prefixes
+// first), so items sharing a prefix (v1..vd) are adjacent; a warp processes
+// 32 consecutive items and reduces the adjoint contributions to shared
+// targets with segmented shuffles.  `head` bit d marks the first item of a
+// run of equal (v1..v_{d+1}) within its warp.
+//
+// Record (16 bytes): idx[0..4] prefix (uint16), idx[5..6] leaves, byte 14 =
+// P | nleaf << 4, byte 15 = head bits.  P == 0 marks padding.
+static constexpr int ITEM_G = 2;
+
+struct ItemSchedule {
+  int K = 0, KP = 0;               // max order, max prefix length (K - 1)
+  int64_t n = 0;                   // items, padded to a multiple of the block size
+  std::vector<uint16_t> rec;       // [n * 8]
+  std::vector<int64_t> kown;       // [n] AA index of the prefix function (-1: none)
+  std::vector<int64_t> kleaf;      // [n * G] AA index of each leaf (-1: none)
+  std::vector<uint8_t> wown, wleaf;
+};
+
+inline ItemSchedule build_items(const Schedule &s, int nthreads) {
+  ItemSchedule it;
+  const int K = s.K;
+  it.K = K;
+  it.KP = K > 1 ? K - 1 : 1;
+  const int KP = it.KP;
+  struct Item { std::vector<int> pre; int64_t kown = -1; uint8_t wown = 0; std::vector<std::pair<int, std::pair<int64_t, uint8_t>>> leaves; };
+  std::map<std::vector<int>, std::vector<Item>> groups;   // prefix -> items (main group, |prefix| == KP)
+  std::map<std::vector<int>, Item> shorts;
+  for (int64_t i = 0; i < s.n; ++i) {
+    const int o = s.ord[i];
+    std::vector<int> t(o);
+    for (int j = 0; j < o; ++j) t[j] = s.v[(size_t)j * s.n + i];
+    if (K > 1 && o == K) {
+      std::vector<int> pre(t.begin(), t.end() - 1);
+      auto &g = groups[pre];
+      if (g.empty() || (int)g.back().leaves.size() == ITEM_G) { g.emplace_back(); g.back().pre = pre; }
+      g.back().leaves.push_back({t.back(), {s.k[i], s.w[i]}});
+    } else if (o == KP) {
+      auto &g = groups[t];
+      if (g.empty()) { g.emplace_back(); g.back().pre = t; }
+      g.front().kown = s.k[i];
+      g.front().wown = s.w[i];
+    } else {
+      Item x; x.pre = t; x.kown = s.k[i]; x.wown = s.w[i];
+      shorts[t] = x;
+    }
+  }
+  std::vector<Item> items;
+  for (auto &kv : groups) for (auto &x : kv.second) items.push_back(x);
+  for (auto &kv : shorts) items.push_back(kv.second);
+  const int64_t n0 = (int64_t)items.size();
+  it.n = ((n0 + nthreads - 1) / nthreads) * nthreads;
+  if (it.n == 0) it.n = nthreads;
+  it.rec.assign((size_t)it.n * 8, 0);
+  it.kown.assign(it.n, -1);
+  it.kleaf.assign((size_t)it.n * ITEM_G, -1);
+  it.wown.assign(it.n, 0);
+  it.wleaf.assign((size_t)it.n * ITEM_G, 0);
+  for (int64_t f = 0; f < n0; ++f) {
+    const Item &x = items[f];
+    uint16_t *r = &it.rec[8 * f];
+    const int P = (int)x.pre.size();
+    for (int d = 0; d < P; ++d) r[d] = (uint16_t)x.pre[d];
+    const int nl = (int)x.leaves.size();
+    for (int g = 0; g < nl; ++g) {
+      ((uint16_t *)r)[5 + g] = (uint16_t)x.leaves[g].first;
+      it.kleaf[(size_t)f * ITEM_G + g] = x.leaves[g].second.first;
+      it.wleaf[(size_t)f * ITEM_G + g] = x.leaves[g].second.second;
+    }
+    it.kown[f] = x.kown;
+    it.wown[f] = x.wown;
+    uint8_t heads = 0;
+    for (int d = 0; d < KP; ++d) {
+      bool head = (f % 32 == 0);
+      if (!head) {
+        const Item &y = items[f - 1];
+        if ((int)y.pre.size() != P || d >= P) head = true;
+        else for (int e = 0; e <= d; ++e) if (y.pre[e] != x.pre[e]) { head = true; break; }
+      }
+      if (head) heads |= (uint8_t)(1u << d);
+    }
+    uint8_t *b = (uint8_t *)r;
+    b[14] = (uint8_t)(P | (nl << 4));
+    b[15] = heads;
+  }
+  for (int64_t f = n0; f < it.n; ++f) ((uint8_t *)&it.rec[8 * f])[15] = 0x1f;  // padding: own segments
+  return it;
+}
+
 }  // namespace ace
