@@ -23,7 +23,7 @@ ACE_ASYNC = 4
 
 EXPORTED = ("ace_ctx_create", "ace_ctx_destroy", "ace_set_params", "ace_set_ctilde",
             "ace_energy_forces", "ace_energy", "ace_basis", "ace_sync", "ace_get_spec_sizes",
-            "ace_last_error_string", "ace_launch_count", "ace_basis_noalloc")
+            "ace_last_error_string", "ace_launch_count", "ace_basis_noalloc", "ace_adjoint_eval_d")
 
 
 class AceError(RuntimeError):
@@ -67,6 +67,7 @@ def load(path: str | None = None):
     lib.ace_energy.argtypes = [P, C.c_int64, P, P, P, P, C.c_int32, P]
     lib.ace_basis.argtypes = [P, C.c_int64, P, P, P, P, P, C.c_int32, P]
     lib.ace_basis_noalloc.argtypes = [P, C.c_int64, P, P, P, P, P]
+    lib.ace_adjoint_eval_d.argtypes = [P, C.c_int64, P, P, P, P, P, C.c_int32, P]
     lib.ace_sync.argtypes = [P]
     lib.ace_get_spec_sizes.argtypes = [P, P]
     lib.ace_last_error_string.argtypes = [P]
@@ -75,7 +76,7 @@ def load(path: str | None = None):
     lib.ace_launch_count.restype = C.c_int64
     for name in ("ace_ctx_create", "ace_ctx_destroy", "ace_set_params", "ace_set_ctilde",
                  "ace_energy_forces", "ace_energy", "ace_basis", "ace_sync", "ace_get_spec_sizes",
-                 "ace_basis_noalloc"):
+                 "ace_basis_noalloc", "ace_adjoint_eval_d"):
         getattr(lib, name).restype = C.c_int
     _lib = lib
     return lib
@@ -187,6 +188,18 @@ class Context:
         self._check(self.lib.ace_basis(self.h, nenv, _ptr(offsets), _ptr(rr), _ptr(sp),
                                        _ptr(B), _ptr(dB), 0, None))
         return (B, dB) if grad else B
+
+    def adjoint_eval_d(self, offsets, rr, w, species=None):
+        """adjoint_EVAL_D: per environment, sum_j w_j . dB/drr_j (nEnv x nB)."""
+        offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+        rr = np.ascontiguousarray(rr, dtype=np.float64).reshape(-1, 3)
+        w = np.ascontiguousarray(w, dtype=np.float64).reshape(-1, 3)
+        sp = None if species is None else np.ascontiguousarray(species, dtype=np.int32)
+        nenv = len(offsets) - 1
+        out = np.empty((nenv, self.spec.nB))
+        self._check(self.lib.ace_adjoint_eval_d(self.h, nenv, _ptr(offsets), _ptr(rr), _ptr(sp), _ptr(w),
+                                                _ptr(out), 0, None))
+        return out
 
     # device-buffer entry point (torch CUDA tensors in and out)
     def energy_forces_device(self, offsets, rr, species, E, G, stream=None, sync=True):

@@ -267,6 +267,7 @@ extern "C" int ace_ctx_destroy(ace_ctx *ctx) {
   for (void *p : ctx->allocs) cudaFree(p);
   if (ctx->d_stage) cudaFree(ctx->d_stage);
   if (ctx->d_scratch) cudaFree(ctx->d_scratch);
+  if (ctx->d_wstage) cudaFree(ctx->d_wstage);
   if (ctx->h_status) cudaFreeHost(ctx->h_status);
   delete ctx;
   return ACE_OK;
@@ -494,7 +495,38 @@ extern "C" int ace_basis(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, con
                                                  {dB, (size_t)nNbr * ctx->nB * 3 * sizeof(double)}};
   return drive(ctx, nEnv, offsets, rr, species, flags, stream, outs,
                [&](const int64_t *o, const double *x, const int32_t *s, std::vector<void *> &d, cudaStream_t st) {
-                 return launch_basis(ctx, nEnv, o, x, s, (double *)d[0], (double *)d[1], st);
+                 int rc = launch_basis(ctx, nEnv, o, x, s, (double *)d[0], nullptr, st);
+                 if (rc || !dB) return rc;
+                 return launch_dbasis(ctx, nEnv, o, offsets, x, s, (double *)d[1], st);
+               });
+}
+
+extern "C" int ace_adjoint_eval_d(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, const double *rr,
+                                  const int32_t *species, const double *w, double *out, int32_t flags,
+                                  void *stream) {
+  if (!ctx) return ACE_ERR_INVALID;
+  if (!out || !w) return ctx_fail(ctx, ACE_ERR_INVALID, "w or out is NULL");
+  if (ctx->nB == 0) return ctx_fail(ctx, ACE_ERR_INVALID, "spec has no U");
+  const bool din = flags & ACE_INPUTS_ON_DEVICE;
+  const double *d_w = w;
+  if (!din) {
+    // host weights: stage them next to the positions (3 per neighbour)
+    const int64_t nNbr = offsets ? offsets[nEnv] : 0;
+    const size_t bytes = std::max<int64_t>(nNbr, 1) * 3 * sizeof(double);
+    ACE_CUDA(cudaSetDevice(ctx->device));
+    if (bytes > ctx->wstage_bytes) {
+      if (ctx->d_wstage) { cudaFree(ctx->d_wstage); ctx->d_wstage = nullptr; ctx->wstage_bytes = 0; }
+      if (cudaMalloc(&ctx->d_wstage, bytes) != cudaSuccess) return ctx_fail(ctx, ACE_ERR_ALLOC, "staging allocation failed");
+      ctx->wstage_bytes = bytes;
+    }
+    if (nNbr > 0)
+      ACE_CUDA(cudaMemcpyAsync(ctx->d_wstage, w, nNbr * 3 * sizeof(double), cudaMemcpyHostToDevice, (cudaStream_t)stream));
+    d_w = (const double *)ctx->d_wstage;
+  }
+  std::vector<std::pair<void *, size_t>> outs = {{out, (size_t)nEnv * ctx->nB * sizeof(double)}};
+  return drive(ctx, nEnv, offsets, rr, species, flags, stream, outs,
+               [&](const int64_t *o, const double *x, const int32_t *s, std::vector<void *> &d, cudaStream_t st) {
+                 return launch_adjoint_eval_d(ctx, nEnv, o, nullptr, x, s, d_w, (double *)d[0], st);
                });
 }
 

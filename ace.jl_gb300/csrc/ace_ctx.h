@@ -66,6 +66,8 @@ struct ace_ctx {
   size_t stage_bytes = 0;
   void *d_scratch = nullptr;
   size_t scratch_bytes = 0;
+  void *d_wstage = nullptr;
+  size_t wstage_bytes = 0;
 
   // launch configuration chosen at create time
   int nt = 128, chunkE = 32, chunkG = 16, npriv = 32, grid = 0;
@@ -84,4 +86,8 @@ int launch_energy_forces(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const d
                          const int32_t *sp, double *E, double *G, cudaStream_t st);
 int launch_basis(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const double *rr,
                  const int32_t *sp, double *B, double *dB, cudaStream_t st);
+int launch_dbasis(ace_ctx *ctx, int64_t nEnv, const int64_t *off_d, const int64_t *off_h, const double *rr,
+                  const int32_t *sp, double *dB, cudaStream_t st);
+int launch_adjoint_eval_d(ace_ctx *ctx, int64_t nEnv, const int64_t *off_d, const int64_t *off_h,
+                          const double *rr, const int32_t *sp, const double *w, double *out, cudaStream_t st);
 }  // namespace ace

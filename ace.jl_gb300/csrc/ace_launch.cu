@@ -126,7 +126,7 @@ static int ensure_scratch(ace_ctx *ctx, size_t bytes) {
 
 int launch_basis(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const double *rr, const int32_t *sp,
                  double *B, double *dB, cudaStream_t st) {
-  if (dB) { ctx->err = "dB is not produced by this build"; return ACE_ERR_UNSUPPORTED; }
+  (void)dB;  // the derivative is produced by launch_dbasis
   if (nEnv == 0) return ACE_OK;
   const bool f32 = (ctx->prec == ACE_PREC_FP32 || ctx->prec == ACE_PREC_FP32_BF16X3);
   const size_t ts = f32 ? 4 : 8;

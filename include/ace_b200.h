@@ -20,6 +20,7 @@
  *                          evaluate_d / evaluate_ed   src/symmbasis.jl:297-336
  *                          (grad_params = B, grad_params_config = dB,
  *                          src/linearmodel.jl:114-128)
+ *   ace_adjoint_eval_d  <- adjoint_EVAL_D(m, cfg, w)  src/evaluator.jl:204-244
  *
  * Many environments are evaluated per call: environment e owns neighbours
  * offsets[e] .. offsets[e+1]-1 of the position array (CSR).  Positions are
@@ -131,6 +132,12 @@ int ace_energy(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, const double 
    dB[(j*nB + b)*3 + a] = dB_b(env of j)/d rr_j[a]. */
 int ace_basis(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, const double *rr,
               const int32_t *species, double *B, double *dB, int32_t flags, void *stream);
+
+/* adjoint_EVAL_D (src/evaluator.jl:204-244): out[e*nB + b] =
+   sum_{j in e} sum_a w[3*j + a] * dB_b/d rr_j[a] -- the mixed derivative used
+   for force matching, without forming dB.  w lives where rr lives (flags). */
+int ace_adjoint_eval_d(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, const double *rr,
+                       const int32_t *species, const double *w, double *out, int32_t flags, void *stream);
 
 /* The symmetric basis B (as ace_basis, without dB) for callers that must not
    allocate device memory while they run -- e.g. an MD engine that owns the

@@ -165,6 +165,19 @@ def test_device_pointer_path(lib, oracle_mod):
     assert relerr(G.cpu().numpy(), Gref) <= 1e-10
 
 
+def test_model_api_gradients(lib, oracle_mod):
+    from ace_gb300.model import LinearACEModel, SymmetricBasis
+    basis = SymmetricBasis(spec=get_spec("test"))
+    c = random_coefficients(basis.spec, seed=5)
+    model = LinearACEModel(basis, c)
+    b = random_batch(4, 10, 10, seed=6)
+    cfgs = [b.env(e)[0] for e in range(4)]
+    dB = model.grad_params_config(cfgs)              # list of (nB, J, 3)
+    g = model.grad_config(cfgs)
+    for e in range(4):
+        assert np.allclose(np.einsum("bjx,b->jx", dB[e], c), g[e], rtol=1e-10, atol=1e-13)
+
+
 def test_model_api(lib, oracle_mod):
     from ace_gb300.model import LinearACEModel, SymmetricBasis
     basis = SymmetricBasis(spec=get_spec("test"))
@@ -183,3 +196,34 @@ def test_model_api(lib, oracle_mod):
     c2 = random_coefficients(basis.spec, seed=7)
     model.set_params(c2)
     assert np.allclose(model.evaluate(cfgs), B @ c2, rtol=1e-11)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32x2", "fp32"])
+@pytest.mark.parametrize("name,nenv,ns", [("test", 20, 1), ("cfg1", 40, 1), ("species", 15, 3)])
+def test_basis_derivative(lib, oracle_mod, prec, name, nenv, ns):
+    """evaluate_ed / grad_params_config: dB_b/drr_j against the oracle."""
+    spec = get_spec(name) if name != "species" else symmetric_basis(3, 6, maxL=6, nspecies=3)
+    b = random_batch(nenv, 8, 20, nspecies=ns, seed=12)
+    orc = oracle_mod.Oracle(spec)
+    Bref, dBref = orc.basis_d(b.offsets, b.rr, b.species)
+    ctx = lib.Context(spec, prec)
+    B, dB = ctx.basis(b.offsets, b.rr, b.species, grad=True)
+    tol = {"fp64": 1e-11, "fp32x2": 1e-11, "fp32": 1e-4}[prec]
+    assert relerr(B, Bref) <= tol * 10
+    assert relerr(dB, dBref) <= tol, relerr(dB, dBref)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_adjoint_eval_d(lib, oracle_mod, prec):
+    """adjoint_EVAL_D (src/evaluator.jl:204-244): sum_j w_j . dB/drr_j."""
+    spec = get_spec("cfg1")
+    b = random_batch(30, 12, 24, seed=21)
+    w = np.random.default_rng(2).standard_normal(b.rr.shape)
+    orc = oracle_mod.Oracle(spec)
+    _, dBref = orc.basis_d(b.offsets, b.rr)
+    ref = np.stack([np.einsum("jbx,jx->b", dBref[b.offsets[e]:b.offsets[e + 1]], w[b.offsets[e]:b.offsets[e + 1]])
+                    for e in range(b.nenv)])
+    ctx = lib.Context(spec, prec)
+    out = ctx.adjoint_eval_d(b.offsets, b.rr, w)
+    tol = {"fp64": 1e-11, "fp32": 1e-4}[prec]
+    assert relerr(out, ref) <= tol, relerr(out, ref)
