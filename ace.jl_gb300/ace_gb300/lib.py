@@ -23,7 +23,8 @@ ACE_ASYNC = 4
 
 EXPORTED = ("ace_ctx_create", "ace_ctx_destroy", "ace_set_params", "ace_set_ctilde",
             "ace_energy_forces", "ace_energy", "ace_basis", "ace_sync", "ace_get_spec_sizes",
-            "ace_last_error_string", "ace_launch_count", "ace_basis_noalloc", "ace_adjoint_eval_d")
+            "ace_last_error_string", "ace_launch_count", "ace_basis_noalloc", "ace_adjoint_eval_d",
+            "ace_set_params_multi", "ace_energy_forces_multi")
 
 
 class AceError(RuntimeError):
@@ -68,6 +69,8 @@ def load(path: str | None = None):
     lib.ace_basis.argtypes = [P, C.c_int64, P, P, P, P, P, C.c_int32, P]
     lib.ace_basis_noalloc.argtypes = [P, C.c_int64, P, P, P, P, P]
     lib.ace_adjoint_eval_d.argtypes = [P, C.c_int64, P, P, P, P, P, C.c_int32, P]
+    lib.ace_set_params_multi.argtypes = [P, P, C.c_int64, C.c_int32]
+    lib.ace_energy_forces_multi.argtypes = [P, C.c_int64, P, P, P, P, P, C.c_int32, P]
     lib.ace_sync.argtypes = [P]
     lib.ace_get_spec_sizes.argtypes = [P, P]
     lib.ace_last_error_string.argtypes = [P]
@@ -76,7 +79,8 @@ def load(path: str | None = None):
     lib.ace_launch_count.restype = C.c_int64
     for name in ("ace_ctx_create", "ace_ctx_destroy", "ace_set_params", "ace_set_ctilde",
                  "ace_energy_forces", "ace_energy", "ace_basis", "ace_sync", "ace_get_spec_sizes",
-                 "ace_basis_noalloc", "ace_adjoint_eval_d"):
+                 "ace_basis_noalloc", "ace_adjoint_eval_d",
+            "ace_set_params_multi", "ace_energy_forces_multi"):
         getattr(lib, name).restype = C.c_int
     _lib = lib
     return lib
@@ -188,6 +192,25 @@ class Context:
         self._check(self.lib.ace_basis(self.h, nenv, _ptr(offsets), _ptr(rr), _ptr(sp),
                                        _ptr(B), _ptr(dB), 0, None))
         return (B, dB) if grad else B
+
+    def set_params_multi(self, c):
+        """c: (nB, nprop) -- one column of coefficients per property."""
+        c = np.asarray(c, dtype=np.float64)
+        cm = np.ascontiguousarray(c.T)
+        self.nprop = cm.shape[0]
+        self._check(self.lib.ace_set_params_multi(self.h, _ptr(cm), cm.shape[1], cm.shape[0]))
+
+    def energy_forces_multi(self, offsets, rr, species=None):
+        """E (nEnv, nprop) and dE/drr (nNbr, nprop, 3)."""
+        offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+        rr = np.ascontiguousarray(rr, dtype=np.float64).reshape(-1, 3)
+        sp = None if species is None else np.ascontiguousarray(species, dtype=np.int32)
+        nenv = len(offsets) - 1
+        E = np.empty((self.nprop, nenv))
+        G = np.empty((self.nprop, len(rr), 3))
+        self._check(self.lib.ace_energy_forces_multi(self.h, nenv, _ptr(offsets), _ptr(rr), _ptr(sp),
+                                                     _ptr(E), _ptr(G), 0, None))
+        return E.T.copy(), G.transpose(1, 0, 2).copy()
 
     def adjoint_eval_d(self, offsets, rr, w, species=None):
         """adjoint_EVAL_D: per environment, sum_j w_j . dB/drr_j (nEnv x nB)."""

@@ -91,7 +91,11 @@ class SymmetricBasis:
 
 
 class LinearACEModel:
-    """E(cfg) = sum_b c_b B_b(cfg), evaluated through c~ = U^T c."""
+    """E(cfg) = sum_b c_b B_b(cfg), evaluated through c~ = U^T c.
+
+    With a 2-D c of shape (nB, nprop) the model has nprop properties
+    (ACE.jl's c::Vector{SVector{N}}, src/linearmodel.jl:28-35): energies come
+    back as (..., nprop) and gradients as (J, nprop, 3)."""
 
     def __init__(self, basis: SymmetricBasis, c=None, evaluator: str = "gpu"):
         if evaluator not in ("gpu", "standard"):
@@ -99,7 +103,22 @@ class LinearACEModel:
         self.basis = basis
         self.c = np.zeros(len(basis)) if c is None else np.array(c, dtype=np.float64)
         self.ctx = Context(basis.spec, basis.precision, basis.device)
-        self.ctx.set_params(self.c)
+        self._push()
+
+    @property
+    def multi(self):
+        return self.c.ndim == 2
+
+    def _push(self):
+        if self.multi:
+            self.ctx.set_params_multi(self.c)
+        else:
+            self.ctx.set_params(self.c)
+
+    def _ef(self, off, rr, sp, forces=True):
+        if self.multi:
+            return self.ctx.energy_forces_multi(off, rr, sp)
+        return self.ctx.energy_forces(off, rr, sp, forces=forces)
 
     def params(self):
         return self.c.copy()
@@ -108,25 +127,27 @@ class LinearACEModel:
         return len(self.c)
 
     def set_params(self, c):
-        self.c[:] = c
-        self.ctx.set_params(self.c)
+        self.c[...] = c
+        self._push()
         return self
 
     def evaluate(self, cfgs):
         single, off, rr, sp = _pack(cfgs)
-        E = self.ctx.energy_forces(off, rr, sp, forces=False)
+        E = self._ef(off, rr, sp, forces=False)
+        if self.multi:
+            E = E[0]
         return E[0] if single else E
 
     def grad_config(self, cfgs):
         single, off, rr, sp = _pack(cfgs)
-        _, G = self.ctx.energy_forces(off, rr, sp)
+        _, G = self._ef(off, rr, sp)
         parts = [G[off[e]:off[e + 1]] for e in range(len(off) - 1)]
         return parts[0] if single else parts
 
     def energy_forces(self, cfgs):
         """Energies and forces F_j = -dE/drr_j in one pass."""
         single, off, rr, sp = _pack(cfgs)
-        E, G = self.ctx.energy_forces(off, rr, sp)
+        E, G = self._ef(off, rr, sp)
         F = [-G[off[e]:off[e + 1]] for e in range(len(off) - 1)]
         return (E[0], F[0]) if single else (E, F)
 

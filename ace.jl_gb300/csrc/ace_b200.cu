@@ -268,6 +268,7 @@ extern "C" int ace_ctx_destroy(ace_ctx *ctx) {
   if (ctx->d_stage) cudaFree(ctx->d_stage);
   if (ctx->d_scratch) cudaFree(ctx->d_scratch);
   if (ctx->d_wstage) cudaFree(ctx->d_wstage);
+  if (ctx->d_ic_multi) cudaFree(ctx->d_ic_multi);
   if (ctx->h_status) cudaFreeHost(ctx->h_status);
   delete ctx;
   return ACE_OK;
@@ -334,6 +335,38 @@ extern "C" int ace_set_params(ace_ctx *ctx, const double *c, int64_t nB) {
     for (int64_t k = ctx->U_indptr[b]; k < ctx->U_indptr[b + 1]; ++k)
       ctx->ctilde[ctx->U_indices[k]] += ctx->U_data[k] * c[b];
   return push_ctilde(ctx);
+}
+
+extern "C" int ace_set_params_multi(ace_ctx *ctx, const double *c, int64_t nB, int32_t nprop) {
+  if (!ctx || !c) return ctx_fail(ctx, ACE_ERR_INVALID, "NULL argument");
+  if (nB != ctx->nB) return ctx_fail(ctx, ACE_ERR_INVALID, "length of c != nB");
+  if (nprop < 1 || nprop > 4096) return ctx_fail(ctx, ACE_ERR_INVALID, "nprop out of range [1, 4096]");
+  if (!ctx->use_items) return ctx_fail(ctx, ACE_ERR_UNSUPPORTED, "multi-property models need the item schedule");
+  ACE_CUDA(cudaSetDevice(ctx->device));
+  ctx->ctilde_multi.assign((size_t)nprop * ctx->nAA, 0.0);
+  for (int p = 0; p < nprop; ++p) {
+    double *ct = ctx->ctilde_multi.data() + (size_t)p * ctx->nAA;
+    const double *cp = c + (size_t)p * nB;
+    for (int64_t b = 0; b < nB; ++b)
+      for (int64_t k = ctx->U_indptr[b]; k < ctx->U_indptr[b + 1]; ++k) ct[ctx->U_indices[k]] += ctx->U_data[k] * cp[b];
+  }
+  const size_t csz = (ctx->prec == ACE_PREC_FP64 || ctx->prec == ACE_PREC_FP32X2) ? 8 : 4;
+  const size_t per = ctx->ik.size() * csz;
+  if (ctx->d_ic_multi && nprop > ctx->nprop) {
+    cudaFree(ctx->d_ic_multi);
+    ctx->d_ic_multi = nullptr;
+  }
+  if (!ctx->d_ic_multi && cudaMalloc(&ctx->d_ic_multi, per * nprop) != cudaSuccess)
+    return ctx_fail(ctx, ACE_ERR_ALLOC, "coefficient allocation failed");
+  ctx->nprop = nprop;
+  for (int p = 0; p < nprop; ++p) {
+    const double *ct = ctx->ctilde_multi.data() + (size_t)p * ctx->nAA;
+    int rc = pack_coefs(ctx, (char *)ctx->d_ic_multi + p * per, (int64_t)ctx->ik.size(), [&](int64_t j) {
+      return ctx->ik[j] < 0 ? 0.0 : ctx->iw[j] * ct[ctx->ik[j]];
+    });
+    if (rc) return rc;
+  }
+  return ACE_OK;
 }
 
 extern "C" int ace_set_ctilde(ace_ctx *ctx, const double *ct, int64_t nAA) {
@@ -475,6 +508,39 @@ extern "C" int ace_energy_forces(ace_ctx *ctx, int64_t nEnv, const int64_t *offs
   return drive(ctx, nEnv, offsets, rr, species, flags, stream, outs,
                [&](const int64_t *o, const double *x, const int32_t *s, std::vector<void *> &d, cudaStream_t st) {
                  return launch_energy_forces(ctx, nEnv, o, x, s, (double *)d[0], (double *)d[1], st);
+               });
+}
+
+extern "C" int ace_energy_forces_multi(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, const double *rr,
+                                       const int32_t *species, double *E, double *dEdrr, int32_t flags,
+                                       void *stream) {
+  if (!ctx) return ACE_ERR_INVALID;
+  if (!E) return ctx_fail(ctx, ACE_ERR_INVALID, "E is NULL");
+  if (ctx->nprop < 1) return ctx_fail(ctx, ACE_ERR_INVALID, "no multi-property coefficients set");
+  const bool din = flags & ACE_INPUTS_ON_DEVICE;
+  if (din && dEdrr && !(flags & ACE_OUTPUTS_ON_DEVICE))
+    return ctx_fail(ctx, ACE_ERR_INVALID, "host gradient output needs host inputs (the size is unknown)");
+  int64_t nNbr = 0;
+  if (!din) nNbr = offsets ? offsets[nEnv] : 0;
+  else if (dEdrr && nEnv > 0) {
+    ACE_CUDA(cudaSetDevice(ctx->device));
+    ACE_CUDA(cudaMemcpy(&nNbr, offsets + nEnv, sizeof(int64_t), cudaMemcpyDeviceToHost));
+  }
+  const int np = ctx->nprop;
+  const size_t csz = (ctx->prec == ACE_PREC_FP64 || ctx->prec == ACE_PREC_FP32X2) ? 8 : 4;
+  const size_t per = ctx->ik.size() * csz;
+  std::vector<std::pair<void *, size_t>> outs = {{E, (size_t)np * nEnv * sizeof(double)},
+                                                 {dEdrr, (size_t)np * nNbr * 3 * sizeof(double)}};
+  return drive(ctx, nEnv, offsets, rr, species, flags, stream, outs,
+               [&](const int64_t *o, const double *x, const int32_t *s, std::vector<void *> &d, cudaStream_t st) {
+                 for (int p = 0; p < np; ++p) {
+                   const double c0 = ctx->has_const ? ctx->ctilde_multi[(size_t)p * ctx->nAA] : 0.0;
+                   double *Ep = (double *)d[0] + (size_t)p * nEnv;
+                   double *Gp = d[1] ? (double *)d[1] + (size_t)p * nNbr * 3 : nullptr;
+                   int rc = launch_energy_forces(ctx, nEnv, o, x, s, Ep, Gp, st, (char *)ctx->d_ic_multi + p * per, c0);
+                   if (rc) return rc;
+                 }
+                 return (int)ACE_OK;
                });
 }
 

@@ -54,6 +54,10 @@ struct ace_ctx {
   void *d_ic = nullptr;        // [(G+1) * item_n] coefficients in the energy type
   std::vector<int64_t> ik;     // [(G+1) * item_n] AA index (-1: none)
   std::vector<uint8_t> iw;     // weights
+  // multi-property coefficient sets (property-major)
+  int nprop = 0;
+  std::vector<double> ctilde_multi;   // [nprop * nAA]
+  void *d_ic_multi = nullptr;         // [nprop * (G+1) * item_n] in the energy type
 
   // host copies
   std::vector<double> ctilde;
@@ -83,7 +87,8 @@ struct ace_ctx {
 namespace ace {
 int kernels_prepare(ace_ctx *ctx);
 int launch_energy_forces(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const double *rr,
-                         const int32_t *sp, double *E, double *G, cudaStream_t st);
+                         const int32_t *sp, double *E, double *G, cudaStream_t st,
+                         const void *ic = nullptr, double c0 = 0.0);
 int launch_basis(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const double *rr,
                  const int32_t *sp, double *B, double *dB, cudaStream_t st);
 int launch_dbasis(ace_ctx *ctx, int64_t nEnv, const int64_t *off_d, const int64_t *off_h, const double *rr,

@@ -104,9 +104,10 @@ int kernels_prepare(ace_ctx *ctx) {
 }
 
 int launch_energy_forces(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const double *rr, const int32_t *sp,
-                         double *E, double *G, cudaStream_t st) {
+                         double *E, double *G, cudaStream_t st, const void *ic, double c0) {
   if (nEnv == 0) return ACE_OK;
   EFArgs a = make_args(ctx, nEnv, off, rr, sp, E, G);
+  if (ic) { a.ic = ic; a.c0 = c0; }
   void *f = ef_func(ctx, G != nullptr);
   const int grid = (int)std::min<int64_t>(nEnv, ctx->grid);
   void *args[] = {&a};

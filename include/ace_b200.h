@@ -118,6 +118,14 @@ int ace_set_params(ace_ctx *ctx, const double *c, int64_t nB);
 /* The AA-basis coefficients c~ directly (length nAA). */
 int ace_set_ctilde(ace_ctx *ctx, const double *ctilde, int64_t nAA);
 
+/* Multi-property models (c::Vector{SVector{N}}, src/linearmodel.jl:28-35):
+   nprop coefficient sets for one basis, property-major c[p*nB + b]. */
+int ace_set_params_multi(ace_ctx *ctx, const double *c, int64_t nB, int32_t nprop);
+/* Energies E[p*nEnv + e] and gradients dEdrr[(p*nNbr + j)*3 + a] of every
+   property set by ace_set_params_multi (property-major outputs). */
+int ace_energy_forces_multi(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, const double *rr,
+                            const int32_t *species, double *E, double *dEdrr, int32_t flags, void *stream);
+
 /* Site energies E[e] and gradients dEdrr[3*j + a] = dE_{e(j)}/d rr_j[a]
    (grad_config; forces on neighbours are -dEdrr).  dEdrr may be NULL.
    species may be NULL for a one-species spec.  `stream` is a cudaStream_t

@@ -227,3 +227,25 @@ def test_adjoint_eval_d(lib, oracle_mod, prec):
     out = ctx.adjoint_eval_d(b.offsets, b.rr, w)
     tol = {"fp64": 1e-11, "fp32": 1e-4}[prec]
     assert relerr(out, ref) <= tol, relerr(out, ref)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32x2"])
+def test_multi_property(lib, oracle_mod, prec):
+    """Multi-property model (c::Vector{SVector{N}}): each property equals the
+    single-property evaluation with that column of coefficients."""
+    from ace_gb300.model import LinearACEModel, SymmetricBasis
+    spec = get_spec("cfg1")
+    rng = np.random.default_rng(8)
+    C3 = np.stack([random_coefficients(spec, seed=s) for s in (1, 2, 3)], axis=1)   # (nB, 3)
+    b = random_batch(50, 12, 24, seed=13)
+    ctx = lib.Context(spec, prec)
+    ctx.set_params_multi(C3)
+    E, G = ctx.energy_forces_multi(b.offsets, b.rr)
+    assert E.shape == (50, 3) and G.shape == (len(b.rr), 3, 3)
+    for p in range(3):
+        Eref, Gref = oracle_mod.Oracle(spec, C3[:, p]).energy_forces(b.offsets, b.rr)
+        assert energy_relerr(E[:, p], Eref) <= TOL[prec]["E"]
+        assert relerr(G[:, p], Gref) <= TOL[prec]["G"]
+    model = LinearACEModel(SymmetricBasis(spec=spec, precision=prec), C3)
+    Em = model.evaluate([b.env(e)[0] for e in range(3)])
+    assert Em.shape == (3, 3) and np.allclose(Em, E[:3], rtol=1e-12)
