@@ -24,7 +24,7 @@ ACE_ASYNC = 4
 EXPORTED = ("ace_ctx_create", "ace_ctx_destroy", "ace_set_params", "ace_set_ctilde",
             "ace_energy_forces", "ace_energy", "ace_basis", "ace_sync", "ace_get_spec_sizes",
             "ace_last_error_string", "ace_launch_count", "ace_basis_noalloc", "ace_adjoint_eval_d",
-            "ace_set_params_multi", "ace_energy_forces_multi")
+            "ace_set_params_multi", "ace_energy_forces_multi", "ace_autotune")
 
 
 class AceError(RuntimeError):
@@ -70,6 +70,7 @@ def load(path: str | None = None):
     lib.ace_basis_noalloc.argtypes = [P, C.c_int64, P, P, P, P, P]
     lib.ace_adjoint_eval_d.argtypes = [P, C.c_int64, P, P, P, P, P, C.c_int32, P]
     lib.ace_set_params_multi.argtypes = [P, P, C.c_int64, C.c_int32]
+    lib.ace_autotune.argtypes = [P, C.c_int64, P, P, P, P, P, C.c_int32, P, P]
     lib.ace_energy_forces_multi.argtypes = [P, C.c_int64, P, P, P, P, P, C.c_int32, P]
     lib.ace_sync.argtypes = [P]
     lib.ace_get_spec_sizes.argtypes = [P, P]
@@ -80,7 +81,7 @@ def load(path: str | None = None):
     for name in ("ace_ctx_create", "ace_ctx_destroy", "ace_set_params", "ace_set_ctilde",
                  "ace_energy_forces", "ace_energy", "ace_basis", "ace_sync", "ace_get_spec_sizes",
                  "ace_basis_noalloc", "ace_adjoint_eval_d",
-            "ace_set_params_multi", "ace_energy_forces_multi"):
+            "ace_set_params_multi", "ace_energy_forces_multi", "ace_autotune"):
         getattr(lib, name).restype = C.c_int
     _lib = lib
     return lib
@@ -230,6 +231,15 @@ class Context:
         st = None if stream is None else C.c_void_p(int(stream))
         self._check(self.lib.ace_energy_forces(self.h, E.numel(), _ptr(offsets), _ptr(rr), _ptr(species),
                                                _ptr(E), _ptr(G), flags, st))
+
+    def autotune(self, offsets, rr, species, E, G, reps=3, stream=None):
+        """Pick the fastest launch configuration on this device batch (torch
+        tensors); returns region_kb + 1000 * (item schedule chosen)."""
+        choice = C.c_int32(0)
+        st = None if stream is None else C.c_void_p(int(stream))
+        self._check(self.lib.ace_autotune(self.h, E.numel(), _ptr(offsets), _ptr(rr), _ptr(species), _ptr(E),
+                                          _ptr(G), reps, st, C.byref(choice)))
+        return int(choice.value)
 
     def sync(self):
         self._check(self.lib.ace_sync(self.h))

@@ -596,6 +596,54 @@ extern "C" int ace_adjoint_eval_d(ace_ctx *ctx, int64_t nEnv, const int64_t *off
                });
 }
 
+// Autotuner: times the energy/force kernel on the caller's batch (device
+// pointers) for each candidate (correlation algorithm x shared-region size)
+// and keeps the fastest.  Returns the chosen configuration in *choice
+// (region_kb + 1000 * use_items) when choice is not NULL.
+extern "C" int ace_autotune(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, const double *rr,
+                            const int32_t *species, double *E, double *dEdrr, int32_t reps, void *stream,
+                            int32_t *choice) {
+  if (!ctx) return ACE_ERR_INVALID;
+  if (!offsets || !rr || !E || nEnv < 1) return ctx_fail(ctx, ACE_ERR_INVALID, "autotune needs a non-empty device batch");
+  if (ctx->nspecies > 1 && !species) return ctx_fail(ctx, ACE_ERR_INVALID, "species required for a multi-species spec");
+  ACE_CUDA(cudaSetDevice(ctx->device));
+  cudaStream_t st = (cudaStream_t)stream;
+  const int regions[] = {16, 24, 32, 40, 48, 64};
+  const bool variants[] = {true, false};
+  float best = 1e30f;
+  int best_region = ctx->region_kb;
+  bool best_items = ctx->use_items;
+  cudaEvent_t e0, e1;
+  ACE_CUDA(cudaEventCreate(&e0));
+  ACE_CUDA(cudaEventCreate(&e1));
+  reps = std::max(1, std::min(reps, 20));
+  for (bool items : variants) {
+    for (int reg : regions) {
+      ctx->use_items = items;
+      ctx->region_kb = reg;
+      if (kernels_prepare(ctx) != ACE_OK) continue;
+      const int32_t *sp = ctx->nspecies > 1 ? species : nullptr;
+      int rc = launch_energy_forces(ctx, nEnv, offsets, rr, sp, E, dEdrr, st);  // warm-up
+      if (rc) continue;
+      cudaEventRecord(e0, st);
+      for (int r = 0; r < reps; ++r) launch_energy_forces(ctx, nEnv, offsets, rr, sp, E, dEdrr, st);
+      cudaEventRecord(e1, st);
+      cudaEventSynchronize(e1);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (cudaGetLastError() == cudaSuccess && ms < best) { best = ms; best_region = reg; best_items = items; }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  ctx->use_items = best_items;
+  ctx->region_kb = best_region;
+  int rc = kernels_prepare(ctx);
+  if (rc) return rc;
+  if (choice) *choice = best_region + (best_items ? 1000 : 0);
+  return read_status(ctx, st);
+}
+
 extern "C" int ace_sync(ace_ctx *ctx) {
   if (!ctx) return ACE_ERR_INVALID;
   ACE_CUDA(cudaSetDevice(ctx->device));

@@ -73,7 +73,8 @@ struct ace_ctx {
   void *d_wstage = nullptr;
   size_t wstage_bytes = 0;
 
-  // launch configuration chosen at create time
+  // launch configuration chosen at create time (and by ace_autotune)
+  int region_kb = 40;          // shared region for neighbour slabs / private adjoint bins
   int nt = 128, chunkE = 32, chunkG = 16, npriv = 32, grid = 0;
   size_t smem = 0;
   int aa_chunk = 32, aa_grid = 0;

@@ -58,9 +58,9 @@ int kernels_prepare(ace_ctx *ctx) {
   bool same;
   type_sizes(ctx, sE, sG, same);
   ctx->nt = NT;
-  // one ~40 KB region holds the neighbour slabs (phases 1, 3) or the private
-  // adjoint bins (phase 2)
-  const int region = 40 * 1024;
+  // one region (ctx->region_kb) holds the neighbour slabs (phases 1, 3) or the
+  // private adjoint bins (phase 2); smaller regions raise occupancy
+  const int region = ctx->region_kb * 1024;
   const int slabE = (ctx->nR + size_p(ctx->L) + 2 * size_y(ctx->L)) * sE;
   const int slabG = (2 * ctx->nR + 2 * size_p(ctx->L) + 8 * size_y(ctx->L)) * sG;
   ctx->chunkE = std::max(1, std::min(64, region / slabE));

@@ -281,9 +281,12 @@ def main():
     ctx32.set_params(c)
     t32p, _ = timed(ctx32, args.steps, args.warmup)
     err32 = errors()
-    # the chosen form: double-float energy path, FP32 adjoint and forces
+    # the chosen form: double-float energy path, FP32 adjoint and forces,
+    # launch configuration picked by the autotuner on this batch
     ctx = Context(spec, CHOSEN, device=local)
     ctx.set_params(c)
+    tuned = ctx.autotune(off_d, rr_d, None, E_d, G_d, reps=1, stream=stream.cuda_stream)
+    torch.cuda.synchronize()
     with Clocks(local) as clk:
         t32, launches = timed(ctx, args.steps, args.warmup)
     clocks = clk.summary()
@@ -345,7 +348,8 @@ def main():
             "vs_baseline": None, "dtype": "f32x2", "data": "synthetic (seeded)",
             "config": {"workload": WORKLOAD["name"], "nenv_per_gpu": nenv, "nnbr_per_gpu": nnbr,
                        "form": "fp32x2: Rn, Ylm, A and the AA energy in double-float (FP32 pairs), adjoint and forces in FP32",
-                       "l2": "flushed (256 MB write) between timed steps", "parallelism": f"replicas x{world}"},
+                       "l2": "flushed (256 MB write) between timed steps", "parallelism": f"replicas x{world}",
+                       "autotuned": {"region_kb": tuned % 1000, "schedule": "items" if tuned >= 1000 else "trie"}},
             "forms": {"fp64": {"value": nenv * k64 * world / t64, "ms_per_step": 1e3 * t64 / k64},
                       "fp32": {"value": nenv * args.steps * world / t32p, "ms_per_step": 1e3 * t32p / args.steps,
                                "error": err32},

@@ -162,6 +162,16 @@ int ace_adjoint_eval_d(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, const
 int ace_basis_noalloc(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, const double *rr,
                       const int32_t *species, double *B, void *stream);
 
+/* Autotuner: times the energy/force kernel on a representative batch (device
+   pointers; E and dEdrr are overwritten) for each candidate launch
+   configuration -- correlation algorithm (item schedule or trie walk) and
+   shared-memory region size -- and keeps the fastest for this context.
+   *choice (optional) receives region_kb + 1000 * (item schedule chosen).
+   No counterpart in the reference (a GPU launch-configuration choice). */
+int ace_autotune(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, const double *rr,
+                 const int32_t *species, double *E, double *dEdrr, int32_t reps, void *stream,
+                 int32_t *choice);
+
 /* Wait for the context's outstanding work; returns the kernels' status. */
 int ace_sync(ace_ctx *ctx);
 

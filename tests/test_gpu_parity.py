@@ -249,3 +249,50 @@ def test_multi_property(lib, oracle_mod, prec):
     model = LinearACEModel(SymmetricBasis(spec=spec, precision=prec), C3)
     Em = model.evaluate([b.env(e)[0] for e in range(3)])
     assert Em.shape == (3, 3) and np.allclose(Em, E[:3], rtol=1e-12)
+
+
+def test_autotune_keeps_results(lib, oracle_mod):
+    torch = pytest.importorskip("torch")
+    spec = get_spec("cfg1")
+    c = random_coefficients(spec, seed=3)
+    b = random_batch(2000, 12, 24, seed=8)
+    Eref, Gref = oracle_mod.Oracle(spec, c).energy_forces(b.offsets, b.rr)
+    ctx = lib.Context(spec, "fp32x2")
+    ctx.set_params(c)
+    off = torch.from_numpy(b.offsets).cuda(); rr = torch.from_numpy(b.rr).cuda()
+    E = torch.empty(b.nenv, dtype=torch.float64, device="cuda"); G = torch.empty_like(rr)
+    choice = ctx.autotune(off, rr, None, E, G, reps=1)
+    assert choice % 1000 in (16, 24, 32, 40, 48, 64)
+    E2, G2 = ctx.energy_forces(b.offsets, b.rr)
+    assert energy_relerr(E2, Eref) <= TOL["fp32x2"]["E"]
+    assert relerr(G2, Gref) <= TOL["fp32x2"]["G"]
+
+
+def test_cuda_graph_capture(lib, oracle_mod):
+    """The device-pointer call (no synchronisation, no allocation) can be
+    captured into a CUDA graph and replayed on new positions."""
+    torch = pytest.importorskip("torch")
+    spec = get_spec("cfg1")
+    c = random_coefficients(spec, seed=3)
+    b = random_batch(500, 12, 24, seed=8)
+    ctx = lib.Context(spec, "fp64")
+    ctx.set_params(c)
+    off = torch.from_numpy(b.offsets).cuda(); rr = torch.from_numpy(b.rr).cuda()
+    E = torch.empty(b.nenv, dtype=torch.float64, device="cuda"); G = torch.empty_like(rr)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        ctx.energy_forces_device(off, rr, None, E, G, stream=s.cuda_stream, sync=False)  # warm-up, outside capture
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        ctx.energy_forces_device(off, rr, None, E, G, stream=s.cuda_stream, sync=False)
+    b2 = random_batch(500, 12, 24, seed=9)
+    # same neighbour counts are required for a replay: reuse the offsets, move the positions
+    rr2 = b2.rr[:len(b.rr)] if len(b2.rr) >= len(b.rr) else np.resize(b2.rr, b.rr.shape)
+    rr.copy_(torch.from_numpy(np.ascontiguousarray(rr2)))
+    g.replay()
+    torch.cuda.synchronize()
+    ctx.sync()
+    Eref, Gref = oracle_mod.Oracle(spec, c).energy_forces(b.offsets, rr2)
+    assert energy_relerr(E.cpu().numpy(), Eref) <= 1e-12
+    assert relerr(G.cpu().numpy(), Gref) <= 1e-10
