@@ -49,6 +49,7 @@ static std::vector<double> coef_table(const ace_spec_bundle *s, int L) {
   t.insert(t.end(), s->rB, s->rB + s->nR);
   t.insert(t.end(), s->rC, s->rC + s->nR);
   std::vector<double> A(szP, 0.0), B(szP, 0.0), C(L + 1, 0.0), D(L + 1, 0.0);
+  if (L >= 1) { C[1] = std::sqrt(3.0); D[1] = -std::sqrt(1.5); }
   for (int l = 2; l <= L; ++l) {
     double ls = double(l * l), lm1s = double((l - 1) * (l - 1));
     for (int m = 0; m <= l - 2; ++m) {

@@ -47,7 +47,7 @@ __global__ void __launch_bounds__(256) daa_kernel(DArgs d) {
   int *ssp = (int *)(sm + lay.spc);
   T *slab = (T *)(sm + lay.slab);
   const int tid = threadIdx.x, nt = blockDim.x;
-  const int szP = size_p(a.L), nY = size_y(a.L);
+  const int nY = size_y(a.L);
   const int SG = lay.slabG;
   for (int i = tid; i < a.ntab; i += nt) tab[i] = load_table<T>(a.tabE, i);
   for (int i = tid; i < a.nA; i += nt) { s_an[i] = a.an[i]; s_aiy[i] = a.aiy[i]; s_amu[i] = a.amu[i]; }
@@ -67,34 +67,39 @@ __global__ void __launch_bounds__(256) daa_kernel(DArgs d) {
     build_A<T>(a, tb, o0, J, d.chunk, lay.slabE, s_an, s_aiy, s_amu, ssp, slab, AE);
     if (!DB)
       for (int i = tid; i < a.nA; i += nt) Dw[i] = {T(0), T(0)};
+    const int LP1 = a.L + 1;
+    const int cj = tid / LP1, cm = tid - cj * LP1;
     for (int c0 = 0; c0 < J; c0 += d.chunk) {
       const int nc = min(d.chunk, J - c0);
       __syncthreads();
-      if (tid < nc) {
-        const int64_t j = o0 + c0 + tid;
+      if (cj < nc) {
+        const int64_t j = o0 + c0 + cj;
         const T x = T(a.rr[3 * j]), y = T(a.rr[3 * j + 1]), z = T(a.rr[3 * j + 2]);
-        int s = 0;
-        if (a.nspecies > 1) {
-          s = a.sp[j];
-          if (s < 0 || s >= a.nspecies) s = -1;
-        }
-        ssp[tid] = s;
-        const T r = sqrt(x * x + y * y + z * z);
-        T *sl = slab + (size_t)tid * SG;
-        cpx<T> *Y = (cpx<T> *)(sl + 2 * a.nR + 2 * szP);
+        const Angles<T> g = angles(x, y, z);
+        T *sl = slab + (size_t)cj * SG;
+        cpx<T> *Y = (cpx<T> *)(sl + 2 * a.nR);
         cpx<T> *dY = Y + nY;
-        radial_eval<T, true>(tb, r, sl, sl + a.nR);
-        sh_grad<T>(tb, x, y, z, sl + 2 * a.nR, sl + 2 * a.nR + szP, Y, dY);
-        const T ux = x / r, uy = y / r, uz = z / r;
-        spos[4 * tid + 0] = ux; spos[4 * tid + 1] = uy; spos[4 * tid + 2] = uz;
-        if (!DB) {
-          // contract the weights now: s = w . rhat, dY[.][0] <- w . grad Y
-          const T w0 = T(d.w[3 * j]), w1 = T(d.w[3 * j + 1]), w2 = T(d.w[3 * j + 2]);
-          spos[4 * tid + 3] = w0 * ux + w1 * uy + w2 * uz;
-          for (int iy = 0; iy < nY; ++iy) {
-            cpx<T> *g = dY + 3 * iy;
-            g[0] = {w0 * g[0].re + w1 * g[1].re + w2 * g[2].re, w0 * g[0].im + w1 * g[1].im + w2 * g[2].im};
+        if (cm == 0) {
+          int s = 0;
+          if (a.nspecies > 1) {
+            s = a.sp[j];
+            if (s < 0 || s >= a.nspecies) s = -1;
           }
+          ssp[cj] = s;
+          const T ux = x / g.r, uy = y / g.r, uz = z / g.r;
+          spos[4 * cj + 0] = ux; spos[4 * cj + 1] = uy; spos[4 * cj + 2] = uz;
+          if (!DB) spos[4 * cj + 3] = T(d.w[3 * j]) * ux + T(d.w[3 * j + 1]) * uy + T(d.w[3 * j + 2]) * uz;
+          radial_eval<T, true>(tb, g.r, sl, sl + a.nR);
+        }
+        sh_col_grad<T>(tb, g, cm, Y, dY);
+        if (!DB) {
+          // contract the weights into this column's entries: dY[.][0] <- w . grad Y
+          const T w0 = T(d.w[3 * j]), w1 = T(d.w[3 * j + 1]), w2 = T(d.w[3 * j + 2]);
+          for (int l = cm; l <= a.L; ++l)
+            for (int sg = (cm == 0 ? 1 : -1); sg <= 1; sg += 2) {
+              cpx<T> *q = dY + 3 * idx_y(l, sg * cm);
+              q[0] = {w0 * q[0].re + w1 * q[1].re + w2 * q[2].re, w0 * q[0].im + w1 * q[1].im + w2 * q[2].im};
+            }
         }
       }
       __syncthreads();
@@ -105,7 +110,7 @@ __global__ void __launch_bounds__(256) daa_kernel(DArgs d) {
           for (int jj = 0; jj < nc; ++jj) {
             if (a.nspecies > 1 && ssp[jj] != mu) continue;
             const T *sl = slab + (size_t)jj * SG;
-            const cpx<T> *Y = (const cpx<T> *)(sl + 2 * a.nR + 2 * szP);
+            const cpx<T> *Y = (const cpx<T> *)(sl + 2 * a.nR);
             const cpx<T> g = (Y + nY)[3 * iy];
             const T dRs = sl[a.nR + n] * spos[4 * jj + 3];
             acc = cadd(acc, cadd(cscale(Y[iy], dRs), cscale(g, sl[n])));
@@ -125,7 +130,7 @@ __global__ void __launch_bounds__(256) daa_kernel(DArgs d) {
           for (int t = ord - 1; t >= 0; --t) { adj[t] = cmul(adj[t], suf); suf = cmul(suf, AE[v[t]]); }
           for (int jj = 0; jj < nc; ++jj) {
             const T *sl = slab + (size_t)jj * SG;
-            const cpx<T> *Y = (const cpx<T> *)(sl + 2 * a.nR + 2 * szP);
+            const cpx<T> *Y = (const cpx<T> *)(sl + 2 * a.nR);
             const cpx<T> *dY = Y + nY;
             const int sp = ssp[jj];
             T g0 = T(0), g1 = T(0), g2 = T(0);
@@ -197,8 +202,8 @@ template <typename T, bool DB>
 static int run_daa(ace_ctx *ctx, int64_t nEnv, const int64_t *off_d, const int64_t *off_h, const double *rr,
                    const int32_t *sp, const double *w, double *out, cudaStream_t st) {
   const size_t ts = sizeof(T);
-  const int slabG = (2 * ctx->nR + 2 * size_p(ctx->L) + 8 * size_y(ctx->L)) * (int)ts;
-  int chunk = std::max(1, std::min(32, (48 * 1024) / slabG));
+  const int slabG = (2 * ctx->nR + 8 * size_y(ctx->L)) * (int)ts;
+  int chunk = std::max(1, std::min(std::min(32, 256 / (ctx->L + 1)), (48 * 1024) / slabG));
   EFLayout lay = ef_layout(ctx->ntab, ctx->nR, ctx->L, ctx->nA, chunk, chunk, 0, 256, (int)ts, (int)ts, true);
   void *f = (void *)daa_kernel<T, DB>;
   if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lay.total) != cudaSuccess) {

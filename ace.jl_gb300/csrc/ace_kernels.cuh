@@ -87,8 +87,8 @@ inline __host__ __device__ EFLayout ef_layout(int ntab, int nR, int L, int nA, i
   const int ch = chunkE > chunkG ? chunkE : chunkG;
   l.pos = o; o = al16(o + (size_t)ch * 4 * sG);
   l.spc = o; o = al16(o + (size_t)ch * 4);
-  l.slabE = nR + szP + 2 * nY;
-  l.slabG = 2 * nR + 2 * szP + 8 * nY;
+  l.slabE = nR + 2 * nY;          // R, Y
+  l.slabG = 2 * nR + 8 * nY;      // R, dR, Y, dY
   // the neighbour slabs (phases 1, 3) and the private adjoint bins (phase 2)
   // are never live at the same time and share one region
   const size_t bE = (size_t)chunkE * l.slabE * sE, bG = (size_t)chunkG * l.slabG * sG;
@@ -134,41 +134,47 @@ __device__ __forceinline__ double block_sum(double v, double *red) {
 }
 
 // Phase 1: A (type T) for the environment's neighbours rr[o0 .. o0+J).
+// Neighbours are staged `chunk` at a time; thread (jj, m) = (t / (L+1),
+// t % (L+1)) evaluates column m of Y for neighbour jj (and R_n when m == 0),
+// then one thread per A entry accumulates.  Requires chunk * (L+1) <= blockDim.
 template <typename T>
 __device__ __forceinline__ void build_A(const EFArgs &a, const Tables<T> &tb, int64_t o0, int J, int chunk,
                                         int SE, const int16_t *s_an, const int16_t *s_aiy, const int16_t *s_amu,
                                         int *ssp, T *slab, cpx<T> *A) {
   const int tid = threadIdx.x, nt = blockDim.x;
-  const int szP = size_p(a.L);
+  const int LP1 = a.L + 1;
+  const int jj = tid / LP1, m = tid - jj * LP1;
   for (int i = tid; i < a.nA; i += nt) A[i] = {Arith<T>::zero(), Arith<T>::zero()};
   for (int c0 = 0; c0 < J; c0 += chunk) {
     const int nc = min(chunk, J - c0);
     __syncthreads();
-    if (tid < nc) {
-      const int64_t j = o0 + c0 + tid;
+    if (jj < nc) {
+      const int64_t j = o0 + c0 + jj;
       const double xd = a.rr[3 * j], yd = a.rr[3 * j + 1], zd = a.rr[3 * j + 2];
-      int s = 0;
-      if (a.nspecies > 1) {
-        s = a.sp[j];
-        if (s < 0 || s >= a.nspecies) { atomicOr(a.status, ACE_STATUS_BAD_SPECIES); s = -1; }
-      }
-      ssp[tid] = s;
-      const double rd = sqrt(xd * xd + yd * yd + zd * zd);
-      if (!(rd > 0.0) || !isfinite(rd)) atomicOr(a.status, ACE_STATUS_BAD_POSITION);
       const T x = Arith<T>::from(xd), y = Arith<T>::from(yd), z = Arith<T>::from(zd);
-      const T r = Arith<T>::sqrt_(x * x + y * y + z * z);
-      T *sl = slab + (size_t)tid * SE;
-      radial_eval<T, false>(tb, r, sl, nullptr);
-      sh_values<T>(tb, x, y, z, sl + a.nR, (cpx<T> *)(sl + a.nR + szP));
+      const Angles<T> g = angles(x, y, z);
+      T *sl = slab + (size_t)jj * SE;
+      if (m == 0) {
+        int s = 0;
+        if (a.nspecies > 1) {
+          s = a.sp[j];
+          if (s < 0 || s >= a.nspecies) { atomicOr(a.status, ACE_STATUS_BAD_SPECIES); s = -1; }
+        }
+        ssp[jj] = s;
+        const double rd = sqrt(xd * xd + yd * yd + zd * zd);
+        if (!(rd > 0.0) || !isfinite(rd)) atomicOr(a.status, ACE_STATUS_BAD_POSITION);
+        radial_eval<T, false>(tb, g.r, sl, nullptr);
+      }
+      sh_col_values<T>(tb, g, m, (cpx<T> *)(sl + a.nR));
     }
     __syncthreads();
     for (int i = tid; i < a.nA; i += nt) {
       const int n = s_an[i], iy = s_aiy[i], mu = s_amu[i];
       cpx<T> acc = A[i];
-      for (int jj = 0; jj < nc; ++jj) {
-        if (a.nspecies > 1 && ssp[jj] != mu) continue;
-        const T *sl = slab + (size_t)jj * SE;
-        const cpx<T> Y = ((const cpx<T> *)(sl + a.nR + szP))[iy];
+      for (int q = 0; q < nc; ++q) {
+        if (a.nspecies > 1 && ssp[q] != mu) continue;
+        const T *sl = slab + (size_t)q * SE;
+        const cpx<T> Y = ((const cpx<T> *)(sl + a.nR))[iy];
         acc = cadd(acc, cscale(Y, sl[n]));
       }
       A[i] = acc;
@@ -202,7 +208,7 @@ __global__ void __launch_bounds__(NT) ef_kernel(EFArgs a) {
   int *ssp = (int *)(sm + lay.spc);
   double *red = (double *)(sm + lay.red);
   const int tid = threadIdx.x;
-  const int szP = size_p(a.L), nY = size_y(a.L);
+  const int nY = size_y(a.L);
   const int npriv = a.npriv;
 
   for (int i = tid; i < a.ntab; i += NT) {
@@ -389,29 +395,33 @@ __global__ void __launch_bounds__(NT) ef_kernel(EFArgs a) {
     const int lane = tid & 31, w = tid >> 5, nw = NT >> 5;
     TG *slab = (TG *)(sm + lay.slab);
     const int SG = lay.slabG;
+    const int LP1 = a.L + 1;
+    const int cj = tid / LP1, cm = tid - cj * LP1;
     for (int c0 = 0; c0 < J; c0 += a.chunkG) {
       const int nc = min(a.chunkG, J - c0);
       __syncthreads();
-      if (tid < nc) {
-        const int64_t j = o0 + c0 + tid;
+      if (cj < nc) {
+        const int64_t j = o0 + c0 + cj;
         const TG x = TG(a.rr[3 * j]), y = TG(a.rr[3 * j + 1]), z = TG(a.rr[3 * j + 2]);
-        int s = 0;
-        if (a.nspecies > 1) {
-          s = a.sp[j];
-          if (s < 0 || s >= a.nspecies) s = -1;
+        const Angles<TG> g = angles(x, y, z);
+        TG *sl = slab + (size_t)cj * SG;
+        cpx<TG> *Yc = (cpx<TG> *)(sl + 2 * a.nR);
+        if (cm == 0) {
+          int s = 0;
+          if (a.nspecies > 1) {
+            s = a.sp[j];
+            if (s < 0 || s >= a.nspecies) s = -1;
+          }
+          ssp[cj] = s;
+          spos[4 * cj + 0] = x / g.r; spos[4 * cj + 1] = y / g.r; spos[4 * cj + 2] = z / g.r;
+          radial_eval<TG, true>(tbG, g.r, sl, sl + a.nR);
         }
-        ssp[tid] = s;
-        const TG r = sqrt(x * x + y * y + z * z);
-        spos[4 * tid + 0] = x / r; spos[4 * tid + 1] = y / r; spos[4 * tid + 2] = z / r;
-        TG *sl = slab + (size_t)tid * SG;
-        radial_eval<TG, true>(tbG, r, sl, sl + a.nR);
-        sh_grad<TG>(tbG, x, y, z, sl + 2 * a.nR, sl + 2 * a.nR + szP, (cpx<TG> *)(sl + 2 * a.nR + 2 * szP),
-                    (cpx<TG> *)(sl + 2 * a.nR + 2 * szP) + nY);
+        sh_col_grad<TG>(tbG, g, cm, Yc, Yc + nY);
       }
       __syncthreads();
       for (int jj = w; jj < nc; jj += nw) {
         const TG *sl = slab + (size_t)jj * SG;
-        const cpx<TG> *Y = (const cpx<TG> *)(sl + 2 * a.nR + 2 * szP);
+        const cpx<TG> *Y = (const cpx<TG> *)(sl + 2 * a.nR);
         const cpx<TG> *dY = Y + nY;
         const int s = ssp[jj];
         TG g0 = TG(0), g1 = TG(0), g2 = TG(0), gr = TG(0);

@@ -61,10 +61,12 @@ int kernels_prepare(ace_ctx *ctx) {
   // one region (ctx->region_kb) holds the neighbour slabs (phases 1, 3) or the
   // private adjoint bins (phase 2); smaller regions raise occupancy
   const int region = ctx->region_kb * 1024;
-  const int slabE = (ctx->nR + size_p(ctx->L) + 2 * size_y(ctx->L)) * sE;
-  const int slabG = (2 * ctx->nR + 2 * size_p(ctx->L) + 8 * size_y(ctx->L)) * sG;
-  ctx->chunkE = std::max(1, std::min(64, region / slabE));
-  ctx->chunkG = std::max(1, std::min(32, region / slabG));
+  // column-parallel 1p basis: (L+1) threads per neighbour
+  const int slabE = (ctx->nR + 2 * size_y(ctx->L)) * sE;
+  const int slabG = (2 * ctx->nR + 8 * size_y(ctx->L)) * sG;
+  const int lanes = NT / (ctx->L + 1);
+  ctx->chunkE = std::max(1, std::min(lanes, region / slabE));
+  ctx->chunkG = std::max(1, std::min(lanes, region / slabG));
   ctx->npriv = std::max(1, std::min(ctx->nA, region / (NT * 2 * sG)));
   EFLayout lay = ef_layout(ctx->ntab, ctx->nR, ctx->L, ctx->nA, ctx->chunkE, ctx->chunkG, ctx->npriv, NT, sE, sG, same);
   while (lay.total > (size_t)ctx->smem_optin && (ctx->chunkE > 1 || ctx->chunkG > 1 || ctx->npriv > 1)) {
@@ -89,7 +91,7 @@ int kernels_prepare(ace_ctx *ctx) {
   }
   ctx->grid = ctx->nsm * std::max(occ, 1);
   // basis path (AA materialisation)
-  ctx->aa_chunk = std::max(1, std::min(64, (32 * 1024) / slabE));
+  ctx->aa_chunk = std::max(1, std::min(256 / (ctx->L + 1), (32 * 1024) / slabE));
   EFLayout la = ef_layout(ctx->ntab, ctx->nR, ctx->L, ctx->nA, ctx->aa_chunk, 1, 0, 256, sE, sE, true);
   ctx->aa_smem = la.total;
   void *fa = aa_func(ctx);

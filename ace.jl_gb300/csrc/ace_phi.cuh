@@ -226,4 +226,128 @@ __device__ __forceinline__ void sh_grad(const Tables<T> &tb, T x, T y, T z, T *P
   }
 }
 
+// ---------------------------------------------------------------------------
+// Column-parallel spherical harmonics: one thread per (neighbour, m), m = 0..L.
+// The associated Legendre recursion of sphericalharmonics.jl:167-267 is a
+// recurrence in l for each fixed m, seeded from the diagonal P(m, m)
+// (itself a short recurrence in m), so each column m is computed in
+// registers by its own thread: seed, P(m+1, m) = sqrt(2m+3) cos(theta) P(m, m),
+// then the three-term recurrence.  Each thread writes Y(l, +-m) (and dY) for
+// l = m..L.  Same formulas and constants as sh_values / sh_grad.
+
+template <typename T> struct Angles { T cost, sint, cosp, sinp, r; };
+
+template <typename T> __device__ __forceinline__ Angles<T> angles(T x, T y, T z) {
+  Angles<T> g;
+  const T rho2 = x * x + y * y;
+  g.r = Arith<T>::sqrt_(rho2 + z * z);
+  const T rho = Arith<T>::sqrt_(rho2);
+  g.cost = z / g.r;
+  g.sint = rho / g.r;
+  g.cosp = Arith<T>::one();
+  g.sinp = Arith<T>::zero();
+  if (Arith<T>::positive(rho)) { g.cosp = x / rho; g.sinp = y / rho; }
+  return g;
+}
+
+// cYlm! (values) for column m
+template <typename T>
+__device__ __forceinline__ void sh_col_values(const Tables<T> &tb, const Angles<T> &g, int m, cpx<T> *Y) {
+  const int L = tb.L;
+  const T zero = Arith<T>::zero();
+  T pmm = tb.sqhalfpi;
+  for (int mm = 1; mm <= m; ++mm) pmm = tb.alpD[mm] * g.sint * pmm;
+  cpx<T> ep = {tb.invsqrt2, zero};
+  const cpx<T> ef = {g.cosp, g.sinp};
+  for (int mm = 1; mm <= m; ++mm) ep = cmul(ep, ef);
+  const cpx<T> em = (m & 1) ? cpx<T>{-ep.re, ep.im} : cpx<T>{ep.re, -ep.im};
+  T p2 = zero, p1 = pmm;
+  for (int l = m; l <= L; ++l) {
+    T p;
+    if (l == m) p = pmm;
+    else if (l == m + 1) p = g.cost * tb.alpC[l] * pmm;
+    else p = tb.alpA[idx_p(l, m)] * (g.cost * p1 + tb.alpB[idx_p(l, m)] * p2);
+    if (l > m) { p2 = p1; p1 = p; }
+    if (m == 0) {
+      Y[idx_y(l, 0)] = {p * tb.invsqrt2, zero};
+    } else {
+      Y[idx_y(l, -m)] = cscale(em, p);
+      Y[idx_y(l, m)] = cscale(ep, p);
+    }
+  }
+}
+
+// cYlm_ed! (values and Cartesian gradients) for column m
+template <typename T>
+__device__ __forceinline__ void sh_col_grad(const Tables<T> &tb, const Angles<T> &g, int m, cpx<T> *Y, cpx<T> *dY) {
+  const int L = tb.L;
+  const T zero = Arith<T>::zero();
+  const T s2 = g.sint * g.sint;
+  const T rinv = Arith<T>::one() / (g.r + Arith<T>::from(2.220446049250313e-16));
+  const T cc = g.cosp * g.cost, sc = g.sinp * g.cost;
+  // seed: P(m, m) (stored divided by sin(theta) for m > 0) and its theta-derivative
+  T t1 = tb.sqhalfpi, td = zero;
+  if (m >= 1) {
+    const T t0 = tb.sqhalfpi;
+    t1 = tb.alpD[1] * t0;
+    td = tb.alpD[1] * (g.cost * t0);
+    for (int l = 2; l <= m; ++l) {
+      const T f = tb.alpD[l];
+      const T nt1 = f * g.sint * t1;
+      const T ntd = f * (g.cost * t1 * g.sint + g.sint * td);
+      t1 = nt1;
+      td = ntd;
+    }
+  }
+  cpx<T> ep = {tb.invsqrt2, zero};
+  const cpx<T> ef = {g.cosp, g.sinp};
+  for (int mm = 1; mm <= m; ++mm) ep = cmul(ep, ef);
+  const cpx<T> em = (m & 1) ? cpx<T>{-ep.re, ep.im} : cpx<T>{ep.re, -ep.im};
+  const T fm = Arith<T>::from((double)m);
+  const cpx<T> dep = {-(fm * ep.im), fm * ep.re};
+  const cpx<T> dem = {fm * em.im, -(fm * em.re)};
+  T p2 = zero, p1 = t1, d2 = zero, d1 = td;
+  for (int l = m; l <= L; ++l) {
+    T p, dp;
+    if (l == m) { p = t1; dp = td; }
+    else if (m == 0) {
+      if (l == 1) { p = g.cost * tb.sq3 * t1; dp = -g.sint * tb.sq3 * t1 + g.cost * tb.sq3 * td; }
+      else {
+        const T A = tb.alpA[idx_p(l, 0)], B = tb.alpB[idx_p(l, 0)];
+        p = A * (g.cost * p1 + B * p2);
+        dp = A * (-g.sint * p1 + g.cost * d1 + B * d2);
+      }
+    } else if (l == m + 1) {
+      const T q = tb.alpC[l];
+      p = q * g.cost * t1;
+      dp = q * (-s2 * t1 + g.cost * td);
+    } else {
+      const T A = tb.alpA[idx_p(l, m)], B = tb.alpB[idx_p(l, m)];
+      p = A * (g.cost * p1 + B * p2);
+      dp = A * (-s2 * p1 + g.cost * d1 + B * d2);
+    }
+    if (l > m) { p2 = p1; p1 = p; d2 = d1; d1 = dp; }
+    if (m == 0) {
+      Y[idx_y(l, 0)] = {p * tb.invsqrt2, zero};
+      const T ft = dp * tb.invsqrt2;
+      cpx<T> *d = dY + 3 * idx_y(l, 0);
+      d[0] = {(cc * ft) * rinv, zero};
+      d[1] = {(sc * ft) * rinv, zero};
+      d[2] = {(-(g.sint * ft)) * rinv, zero};
+    } else {
+      Y[idx_y(l, -m)] = cscale(cscale(em, p), g.sint);
+      Y[idx_y(l, m)] = cscale(cscale(ep, p), g.sint);
+#pragma unroll
+      for (int s = 0; s < 2; ++s) {
+        const cpx<T> fps = cscale(s == 0 ? dem : dep, p);
+        const cpx<T> ft = cscale(s == 0 ? em : ep, dp);
+        cpx<T> *d = dY + 3 * idx_y(l, s == 0 ? -m : m);
+        d[0] = {(-(g.sinp * fps.re) + cc * ft.re) * rinv, (-(g.sinp * fps.im) + cc * ft.im) * rinv};
+        d[1] = {((g.cosp * fps.re) + sc * ft.re) * rinv, ((g.cosp * fps.im) + sc * ft.im) * rinv};
+        d[2] = {(-(g.sint * ft.re)) * rinv, (-(g.sint * ft.im)) * rinv};
+      }
+    }
+  }
+}
+
 }  // namespace ace
