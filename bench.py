@@ -333,7 +333,7 @@ def main():
     fl = flops_per_env(spec, Jmean) * nenv
     achieved = fl / (t32 / args.steps) / 1e12
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", "ef_kernel_fp32_traffic.json")
+    tpath = os.path.join(ROOT, "profiles", "ef_kernel_fp32x2_traffic.json")
     if os.path.exists(tpath):
         tr = json.load(open(tpath))
         traffic = tr["dram_bytes_per_env"] * nenv
