@@ -24,7 +24,9 @@ ACE_ASYNC = 4
 EXPORTED = ("ace_ctx_create", "ace_ctx_destroy", "ace_set_params", "ace_set_ctilde",
             "ace_energy_forces", "ace_energy", "ace_basis", "ace_sync", "ace_get_spec_sizes",
             "ace_last_error_string", "ace_launch_count", "ace_basis_noalloc", "ace_adjoint_eval_d",
-            "ace_set_params_multi", "ace_energy_forces_multi", "ace_autotune")
+            "ace_set_params_multi", "ace_energy_forces_multi", "ace_autotune", "ace_set_radial_mlp",
+            "ace_radial_mlp_params", "ace_radial_mlp_forward", "ace_radial_mlp_backward",
+            "ace_energy_radial_adjoint", "ace_adam_step", "ace_radial_mlp_get_params")
 
 
 class AceError(RuntimeError):
@@ -44,6 +46,11 @@ class SpecBundle(C.Structure):
         ("nAA", C.c_int64), ("maxord", C.c_int32), ("orders", C.c_void_p), ("iAA2iA", C.c_void_p),
         ("nB", C.c_int64), ("U_indptr", C.c_void_p), ("U_indices", C.c_void_p), ("U_data", C.c_void_p),
     ]
+
+
+class RadialMLPDesc(C.Structure):
+    _fields_ = [("version", C.c_int32), ("K", C.c_int32), ("Q", C.c_int32), ("nspecies", C.c_int32),
+                ("H", C.c_int32), ("tmax", C.c_double), ("params", C.c_void_p), ("nparams", C.c_int64)]
 
 
 _lib = None
@@ -72,6 +79,13 @@ def load(path: str | None = None):
     lib.ace_set_params_multi.argtypes = [P, P, C.c_int64, C.c_int32]
     lib.ace_autotune.argtypes = [P, C.c_int64, P, P, P, P, P, C.c_int32, P, P]
     lib.ace_energy_forces_multi.argtypes = [P, C.c_int64, P, P, P, P, P, C.c_int32, P]
+    lib.ace_set_radial_mlp.argtypes = [P, P]
+    lib.ace_radial_mlp_params.argtypes = [P, P, P]
+    lib.ace_radial_mlp_forward.argtypes = [P, C.c_int64, P, P, P, P]
+    lib.ace_radial_mlp_get_params.argtypes = [P, P, C.c_int32]
+    lib.ace_radial_mlp_backward.argtypes = [P, C.c_int64, P, P, P, P, P, P]
+    lib.ace_energy_radial_adjoint.argtypes = [P, C.c_int64, P, P, P, P, P, P, P]
+    lib.ace_adam_step.argtypes = [C.c_int64, P, P, P, P, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int32, P]
     lib.ace_sync.argtypes = [P]
     lib.ace_get_spec_sizes.argtypes = [P, P]
     lib.ace_last_error_string.argtypes = [P]
@@ -81,7 +95,9 @@ def load(path: str | None = None):
     for name in ("ace_ctx_create", "ace_ctx_destroy", "ace_set_params", "ace_set_ctilde",
                  "ace_energy_forces", "ace_energy", "ace_basis", "ace_sync", "ace_get_spec_sizes",
                  "ace_basis_noalloc", "ace_adjoint_eval_d",
-            "ace_set_params_multi", "ace_energy_forces_multi", "ace_autotune"):
+            "ace_set_params_multi", "ace_energy_forces_multi", "ace_autotune", "ace_set_radial_mlp",
+                 "ace_radial_mlp_params", "ace_radial_mlp_forward", "ace_radial_mlp_backward",
+                 "ace_energy_radial_adjoint", "ace_adam_step", "ace_radial_mlp_get_params"):
         getattr(lib, name).restype = C.c_int
     _lib = lib
     return lib
@@ -138,6 +154,7 @@ class Context:
         self.lib = load()
         self.spec = spec
         self.precision = precision
+        self.device = device
         bundle, self._keep = make_bundle(spec)
         h = C.c_void_p()
         rc = self.lib.ace_ctx_create(C.byref(bundle), PREC[precision], device, C.byref(h))
@@ -240,6 +257,44 @@ class Context:
         self._check(self.lib.ace_autotune(self.h, E.numel(), _ptr(offsets), _ptr(rr), _ptr(species), _ptr(E),
                                           _ptr(G), reps, st, C.byref(choice)))
         return int(choice.value)
+
+    # learned radial form (device tensors for the training entry points)
+    def set_radial_mlp(self, params, K, Q, nspecies, tmax, H=64):
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        d = RadialMLPDesc(1, K, Q, nspecies, H, float(tmax), _ptr(p), len(p))
+        self._check(self.lib.ace_set_radial_mlp(self.h, C.byref(d)))
+
+    def radial_mlp_params(self):
+        """(device address, length) of the context's MLP parameters."""
+        ptr, n = C.c_void_p(), C.c_int64()
+        self._check(self.lib.ace_radial_mlp_params(self.h, C.byref(ptr), C.byref(n)))
+        return int(ptr.value), int(n.value)
+
+    def radial_mlp_get_params(self):
+        _, n = self.radial_mlp_params()
+        out = np.empty(n, dtype=np.float32)
+        self._check(self.lib.ace_radial_mlp_get_params(self.h, _ptr(out), 0))
+        return out
+
+    def radial_mlp_forward(self, rr, species, R, stream=None):
+        st = None if stream is None else C.c_void_p(int(stream))
+        self._check(self.lib.ace_radial_mlp_forward(self.h, rr.shape[0], _ptr(rr), _ptr(species), _ptr(R), st))
+
+    def radial_mlp_backward(self, rr, species, gR, wj, gparams, stream=None):
+        st = None if stream is None else C.c_void_p(int(stream))
+        self._check(self.lib.ace_radial_mlp_backward(self.h, rr.shape[0], _ptr(rr), _ptr(species), _ptr(gR),
+                                                     _ptr(wj), _ptr(gparams), st))
+
+    def energy_radial_adjoint(self, offsets, rr, species, E, G, GR, stream=None):
+        st = None if stream is None else C.c_void_p(int(stream))
+        self._check(self.lib.ace_energy_radial_adjoint(self.h, E.numel(), _ptr(offsets), _ptr(rr), _ptr(species),
+                                                       _ptr(E), _ptr(G), _ptr(GR), st))
+
+    def adam_step(self, w, g, m, v, lr, step, beta1=0.9, beta2=0.999, eps=1e-8, stream=None):
+        st = None if stream is None else C.c_void_p(int(stream))
+        w_ptr = C.c_void_p(w) if isinstance(w, int) else _ptr(w)
+        self._check(self.lib.ace_adam_step(g.numel(), w_ptr, _ptr(g), _ptr(m), _ptr(v), lr, beta1, beta2, eps,
+                                           step, st))
 
     def sync(self):
         self._check(self.lib.ace_sync(self.h))

@@ -270,6 +270,8 @@ extern "C" int ace_ctx_destroy(ace_ctx *ctx) {
   if (ctx->d_scratch) cudaFree(ctx->d_scratch);
   if (ctx->d_wstage) cudaFree(ctx->d_wstage);
   if (ctx->d_ic_multi) cudaFree(ctx->d_ic_multi);
+  if (ctx->d_mlp) cudaFree(ctx->d_mlp);
+  if (ctx->d_Rext) cudaFree(ctx->d_Rext);
   if (ctx->h_status) cudaFreeHost(ctx->h_status);
   delete ctx;
   return ACE_OK;
@@ -379,6 +381,10 @@ extern "C" int ace_set_ctilde(ace_ctx *ctx, const double *ct, int64_t nAA) {
 
 // Host-side validation of host inputs (the library never reads outside the
 // CSR extent it is given; device inputs are checked inside the kernels).
+// species an input batch carries: the spec's, or the radial MLP's in the
+// learned form (whose spec is single-species)
+static int input_species(const ace_ctx *ctx) { return ctx->learned ? ctx->mlpS : ctx->nspecies; }
+
 static int validate_inputs(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const double *rr,
                            const int32_t *sp) {
   if (nEnv < 0) return ctx_fail(ctx, ACE_ERR_INVALID, "nEnv < 0");
@@ -393,10 +399,11 @@ static int validate_inputs(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const
     if (x == 0.0 && y == 0.0 && z == 0.0)
       return ctx_fail(ctx, ACE_ERR_INVALID, "neighbour at the centre (r == 0)");
   }
-  if (ctx->nspecies > 1) {
+  const int nsp = input_species(ctx);
+  if (nsp > 1) {
     if (!sp) return ctx_fail(ctx, ACE_ERR_INVALID, "species required for a multi-species spec");
     for (int64_t j = 0; j < n; ++j)
-      if (sp[j] < 0 || sp[j] >= ctx->nspecies) return ctx_fail(ctx, ACE_ERR_INVALID, "species out of range");
+      if (sp[j] < 0 || sp[j] >= nsp) return ctx_fail(ctx, ACE_ERR_INVALID, "species out of range");
   }
   return ACE_OK;
 }
@@ -450,16 +457,17 @@ static int drive(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, const doubl
     int rc = validate_inputs(ctx, nEnv, offsets, rr, species);
     if (rc) return rc;
     nNbr = offsets[nEnv];
-  } else if (ctx->nspecies > 1 && !species) {
+  } else if (input_species(ctx) > 1 && !species) {
     return ctx_fail(ctx, ACE_ERR_INVALID, "species required for a multi-species spec");
   }
+  const int nsp = input_species(ctx);
   // staging: inputs (if host) + outputs (if host)
   size_t need = 0;
   size_t o_off = 0, o_rr = 0, o_sp = 0;
   if (!din) {
     o_off = need; need += al256((nEnv + 1) * sizeof(int64_t));
     o_rr = need; need += al256(std::max<int64_t>(nNbr, 1) * 3 * sizeof(double));
-    if (species && ctx->nspecies > 1) { o_sp = need; need += al256(std::max<int64_t>(nNbr, 1) * sizeof(int32_t)); }
+    if (species && nsp > 1) { o_sp = need; need += al256(std::max<int64_t>(nNbr, 1) * sizeof(int32_t)); }
   }
   std::vector<size_t> o_out(outs_host_bytes.size());
   if (!dout)
@@ -472,13 +480,13 @@ static int drive(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, const doubl
     ACE_CUDA(cudaMemcpyAsync(base + o_rr, rr, nNbr * 3 * sizeof(double), cudaMemcpyHostToDevice, st));
     d_off = (const int64_t *)(base + o_off);
     d_rr = (const double *)(base + o_rr);
-    if (species && ctx->nspecies > 1) {
+    if (species && nsp > 1) {
       ACE_CUDA(cudaMemcpyAsync(base + o_sp, species, nNbr * sizeof(int32_t), cudaMemcpyHostToDevice, st));
       d_sp = (const int32_t *)(base + o_sp);
     } else {
       d_sp = nullptr;
     }
-  } else if (ctx->nspecies == 1) {
+  } else if (nsp == 1) {
     d_sp = nullptr;
   }
   std::vector<void *> d_outs(outs_host_bytes.size());
@@ -606,7 +614,7 @@ extern "C" int ace_autotune(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, 
                             int32_t *choice) {
   if (!ctx) return ACE_ERR_INVALID;
   if (!offsets || !rr || !E || nEnv < 1) return ctx_fail(ctx, ACE_ERR_INVALID, "autotune needs a non-empty device batch");
-  if (ctx->nspecies > 1 && !species) return ctx_fail(ctx, ACE_ERR_INVALID, "species required for a multi-species spec");
+  if (input_species(ctx) > 1 && !species) return ctx_fail(ctx, ACE_ERR_INVALID, "species required for a multi-species spec");
   ACE_CUDA(cudaSetDevice(ctx->device));
   cudaStream_t st = (cudaStream_t)stream;
   const int regions[] = {16, 24, 32, 40, 48, 64};
@@ -623,7 +631,7 @@ extern "C" int ace_autotune(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, 
       ctx->use_items = items;
       ctx->region_kb = reg;
       if (kernels_prepare(ctx) != ACE_OK) continue;
-      const int32_t *sp = ctx->nspecies > 1 ? species : nullptr;
+      const int32_t *sp = input_species(ctx) > 1 ? species : nullptr;
       int rc = launch_energy_forces(ctx, nEnv, offsets, rr, sp, E, dEdrr, st);  // warm-up
       if (rc) continue;
       cudaEventRecord(e0, st);

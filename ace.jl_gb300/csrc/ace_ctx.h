@@ -80,6 +80,19 @@ struct ace_ctx {
   int aa_chunk = 32, aa_grid = 0;
   size_t aa_smem = 0;
 
+  // learned radial form (ace_set_radial_mlp): the spec's radial index n is a
+  // channel k < K of an MLP (transform features, species one-hot) -> K (L+1)
+  // outputs; A entry (n, l, m) reads channel n + K l
+  bool learned = false;
+  int mlpK = 0, mlpQ = 0, mlpS = 0, mlpH = 0, mlpC = 0, mlpD = 0;
+  int64_t mlp_np = 0;
+  double mlp_tmax = 0;
+  float *d_mlp = nullptr;       // parameters [W1 b1 W2 b2 W3 b3]
+  float *d_Rext = nullptr;      // [nNbr][2 C] radial values and r-derivatives
+  int64_t rext_cap = 0;         // neighbours d_Rext can hold
+  int mlp_grid_f = 0, mlp_grid_b = 0;
+  size_t mlp_smem_f = 0, mlp_smem_b = 0;
+
   std::vector<void *> allocs;
   int64_t launches = 0;
   std::string err;
@@ -94,6 +107,14 @@ int launch_basis(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const double *r
                  const int32_t *sp, double *B, double *dB, cudaStream_t st);
 int launch_dbasis(ace_ctx *ctx, int64_t nEnv, const int64_t *off_d, const int64_t *off_h, const double *rr,
                   const int32_t *sp, double *dB, cudaStream_t st);
+// learned radial form (ace_mlp.cu)
+int mlp_prepare(ace_ctx *ctx);
+int mlp_forward(ace_ctx *ctx, int64_t nEnv, const int64_t *off, int64_t nNbr, const double *rr, const int32_t *sp,
+                float *R, cudaStream_t st);
+int learned_radials(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const double *rr, const int32_t *sp,
+                    cudaStream_t st);
+int launch_radial_adjoint(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const double *rr, const int32_t *sp,
+                          double *E, double *G, float *GR, cudaStream_t st);
 int launch_adjoint_eval_d(ace_ctx *ctx, int64_t nEnv, const int64_t *off_d, const int64_t *off_h,
                           const double *rr, const int32_t *sp, const double *w, double *out, cudaStream_t st);
 }  // namespace ace

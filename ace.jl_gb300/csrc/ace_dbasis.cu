@@ -36,7 +36,7 @@ template <typename T, bool DB>
 __global__ void __launch_bounds__(256) daa_kernel(DArgs d) {
   const EFArgs &a = d.a;
   extern __shared__ __align__(16) unsigned char sm[];
-  const EFLayout lay = ef_layout(a.ntab, a.nR, a.L, a.nA, d.chunk, d.chunk, 0, 256, sizeof(T), sizeof(T), true);
+  const EFLayout lay = ef_layout(a.ntab, a.nRs, a.L, a.nA, d.chunk, d.chunk, 0, 256, sizeof(T), sizeof(T), true);
   T *tab = (T *)(sm + lay.tabE);
   int16_t *s_an = (int16_t *)(sm + lay.an);
   int16_t *s_aiy = (int16_t *)(sm + lay.aiy);
@@ -258,6 +258,7 @@ static int run_daa(ace_ctx *ctx, int64_t nEnv, const int64_t *off_d, const int64
 int launch_dbasis(ace_ctx *ctx, int64_t nEnv, const int64_t *off_d, const int64_t *off_h, const double *rr,
                   const int32_t *sp, double *dB, cudaStream_t st) {
   if (nEnv == 0) return ACE_OK;
+  if (ctx->learned) { ctx->err = "basis derivatives are not available in the learned radial form"; return ACE_ERR_UNSUPPORTED; }
   if (ctx->prec == ACE_PREC_FP32 || ctx->prec == ACE_PREC_FP32_BF16X3)
     return run_daa<float, true>(ctx, nEnv, off_d, off_h, rr, sp, nullptr, dB, st);
   return run_daa<double, true>(ctx, nEnv, off_d, off_h, rr, sp, nullptr, dB, st);
@@ -266,6 +267,7 @@ int launch_dbasis(ace_ctx *ctx, int64_t nEnv, const int64_t *off_d, const int64_
 int launch_adjoint_eval_d(ace_ctx *ctx, int64_t nEnv, const int64_t *off_d, const int64_t *off_h,
                           const double *rr, const int32_t *sp, const double *w, double *out, cudaStream_t st) {
   if (nEnv == 0) return ACE_OK;
+  if (ctx->learned) { ctx->err = "basis derivatives are not available in the learned radial form"; return ACE_ERR_UNSUPPORTED; }
   if (ctx->prec == ACE_PREC_FP32 || ctx->prec == ACE_PREC_FP32_BF16X3)
     return run_daa<float, false>(ctx, nEnv, off_d, off_h, rr, sp, w, out, st);
   return run_daa<double, false>(ctx, nEnv, off_d, off_h, rr, sp, w, out, st);

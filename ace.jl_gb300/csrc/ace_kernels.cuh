@@ -45,6 +45,13 @@ struct EFArgs {
   double *G;
   const void *tabE, *tabG;
   int ntab, nR, L, pl, pr, tp;
+  // radial channels held per neighbour in the slabs: nR for the polynomial
+  // basis, K (L+1) for the learned radial form, whose values come from Rext
+  // ([nNbr][2 nRs]: R then dR/dr, written by the radial MLP) instead of the
+  // recursion; GR ([nNbr][nRs], optional) receives dE/dR_n(r_j)
+  int nRs;
+  const float *Rext;
+  float *GR;
   const int16_t *an, *aiy, *amu;
   int nA, nspecies;
   // correlation schedule: interleaved records and coefficients (ace_sched.h)
@@ -72,7 +79,7 @@ struct EFLayout {
 };
 
 inline __host__ __device__ EFLayout ef_layout(int ntab, int nR, int L, int nA, int chunkE, int chunkG,
-                                              int npriv, int nt, int sE, int sG, bool same) {
+                                              int npriv, int nt, int sE, int sG, bool same, bool radj = false) {
   EFLayout l;
   size_t o = 0;
   const int szP = size_p(L), nY = size_y(L);
@@ -88,7 +95,7 @@ inline __host__ __device__ EFLayout ef_layout(int ntab, int nR, int L, int nA, i
   l.pos = o; o = al16(o + (size_t)ch * 4 * sG);
   l.spc = o; o = al16(o + (size_t)ch * 4);
   l.slabE = nR + 2 * nY;          // R, Y
-  l.slabG = 2 * nR + 8 * nY;      // R, dR, Y, dY
+  l.slabG = 2 * nR + 8 * nY + (radj ? nR : 0);  // R, dR, Y, dY [, dE/dR accumulators]
   // the neighbour slabs (phases 1, 3) and the private adjoint bins (phase 2)
   // are never live at the same time and share one region
   const size_t bE = (size_t)chunkE * l.slabE * sE, bG = (size_t)chunkG * l.slabG * sG;
@@ -163,9 +170,11 @@ __device__ __forceinline__ void build_A(const EFArgs &a, const Tables<T> &tb, in
         ssp[jj] = s;
         const double rd = sqrt(xd * xd + yd * yd + zd * zd);
         if (!(rd > 0.0) || !isfinite(rd)) atomicOr(a.status, ACE_STATUS_BAD_POSITION);
-        radial_eval<T, false>(tb, g.r, sl, nullptr);
+        if (!a.Rext) radial_eval<T, false>(tb, g.r, sl, nullptr);
       }
-      sh_col_values<T>(tb, g, m, (cpx<T> *)(sl + a.nR));
+      if (a.Rext)
+        for (int n = m; n < a.nRs; n += LP1) sl[n] = Arith<T>::from((double)a.Rext[(size_t)j * 2 * a.nRs + n]);
+      sh_col_values<T>(tb, g, m, (cpx<T> *)(sl + a.nRs));
     }
     __syncthreads();
     for (int i = tid; i < a.nA; i += nt) {
@@ -174,7 +183,7 @@ __device__ __forceinline__ void build_A(const EFArgs &a, const Tables<T> &tb, in
       for (int q = 0; q < nc; ++q) {
         if (a.nspecies > 1 && ssp[q] != mu) continue;
         const T *sl = slab + (size_t)q * SE;
-        const cpx<T> Y = ((const cpx<T> *)(sl + a.nR))[iy];
+        const cpx<T> Y = ((const cpx<T> *)(sl + a.nRs))[iy];
         acc = cadd(acc, cscale(Y, sl[n]));
       }
       A[i] = acc;
@@ -193,8 +202,8 @@ template <typename TE, typename TG, int K, int NT, bool GRAD, bool ITEMS>
 __global__ void __launch_bounds__(NT) ef_kernel(EFArgs a) {
   constexpr bool SAME = std::is_same<TE, TG>::value;
   extern __shared__ __align__(16) unsigned char sm[];
-  const EFLayout lay = ef_layout(a.ntab, a.nR, a.L, a.nA, a.chunkE, a.chunkG, a.npriv, NT, sizeof(TE),
-                                 sizeof(TG), SAME);
+  const EFLayout lay = ef_layout(a.ntab, a.nRs, a.L, a.nA, a.chunkE, a.chunkG, a.npriv, NT, sizeof(TE),
+                                 sizeof(TG), SAME, a.Rext != nullptr);
   TE *tabE = (TE *)(sm + lay.tabE);
   TG *tabG = (TG *)(sm + lay.tabG);
   int16_t *s_an = (int16_t *)(sm + lay.an);
@@ -405,7 +414,15 @@ __global__ void __launch_bounds__(NT) ef_kernel(EFArgs a) {
         const TG x = TG(a.rr[3 * j]), y = TG(a.rr[3 * j + 1]), z = TG(a.rr[3 * j + 2]);
         const Angles<TG> g = angles(x, y, z);
         TG *sl = slab + (size_t)cj * SG;
-        cpx<TG> *Yc = (cpx<TG> *)(sl + 2 * a.nR);
+        cpx<TG> *Yc = (cpx<TG> *)(sl + 2 * a.nRs);
+        if (a.Rext) {
+          const float *rx = a.Rext + (size_t)j * 2 * a.nRs;
+          for (int n = cm; n < a.nRs; n += LP1) {
+            sl[n] = TG(rx[n]);
+            sl[a.nRs + n] = TG(rx[a.nRs + n]);
+            sl[2 * a.nRs + 8 * nY + n] = TG(0);
+          }
+        }
         if (cm == 0) {
           int s = 0;
           if (a.nspecies > 1) {
@@ -414,24 +431,27 @@ __global__ void __launch_bounds__(NT) ef_kernel(EFArgs a) {
           }
           ssp[cj] = s;
           spos[4 * cj + 0] = x / g.r; spos[4 * cj + 1] = y / g.r; spos[4 * cj + 2] = z / g.r;
-          radial_eval<TG, true>(tbG, g.r, sl, sl + a.nR);
+          if (!a.Rext) radial_eval<TG, true>(tbG, g.r, sl, sl + a.nRs);
         }
         sh_col_grad<TG>(tbG, g, cm, Yc, Yc + nY);
       }
       __syncthreads();
       for (int jj = w; jj < nc; jj += nw) {
-        const TG *sl = slab + (size_t)jj * SG;
-        const cpx<TG> *Y = (const cpx<TG> *)(sl + 2 * a.nR);
+        TG *sl = slab + (size_t)jj * SG;
+        const cpx<TG> *Y = (const cpx<TG> *)(sl + 2 * a.nRs);
         const cpx<TG> *dY = Y + nY;
+        TG *sgr = sl + 2 * a.nRs + 8 * nY;
         const int s = ssp[jj];
         TG g0 = TG(0), g1 = TG(0), g2 = TG(0), gr = TG(0);
         for (int i = lane; i < a.nA; i += 32) {
           if (a.nspecies > 1 && s_amu[i] != s) continue;
           const int n = s_an[i], iy = s_aiy[i];
           const cpx<TG> d = D[i];
-          const TG R = sl[n], dR = sl[a.nR + n];
+          const TG R = sl[n], dR = sl[a.nRs + n];
           const cpx<TG> y0 = Y[iy];
-          gr += dR * (d.re * y0.re - d.im * y0.im);
+          const TG p = d.re * y0.re - d.im * y0.im;
+          gr += dR * p;
+          if (a.GR) atomicAdd(sgr + n, p);
           const cpx<TG> *dy = dY + 3 * iy;
           g0 += R * (d.re * dy[0].re - d.im * dy[0].im);
           g1 += R * (d.re * dy[1].re - d.im * dy[1].im);
@@ -444,11 +464,18 @@ __global__ void __launch_bounds__(NT) ef_kernel(EFArgs a) {
           g2 += __shfl_xor_sync(0xffffffffu, g2, o);
           gr += __shfl_xor_sync(0xffffffffu, gr, o);
         }
-        if (lane == 0) {
+        if (lane == 0 && a.G) {
           const int64_t j = o0 + c0 + jj;
           a.G[3 * j + 0] = (double)(gr * spos[4 * jj + 0] + g0);
           a.G[3 * j + 1] = (double)(gr * spos[4 * jj + 1] + g1);
           a.G[3 * j + 2] = (double)(gr * spos[4 * jj + 2] + g2);
+        }
+      }
+      if (a.GR) {  // dE/dR_n(r_j) of the chunk, written contiguously
+        __syncthreads();
+        for (int q = tid; q < nc * a.nRs; q += NT) {
+          const int jj = q / a.nRs, n = q - jj * a.nRs;
+          a.GR[(size_t)(o0 + c0 + jj) * a.nRs + n] = (float)slab[(size_t)jj * SG + 2 * a.nRs + 8 * nY + n];
         }
       }
     }
@@ -461,7 +488,7 @@ __global__ void __launch_bounds__(NT) ef_kernel(EFArgs a) {
 template <typename TE, typename TO>
 __global__ void __launch_bounds__(256) aa_kernel(EFArgs a) {
   extern __shared__ __align__(16) unsigned char sm[];
-  const EFLayout lay = ef_layout(a.ntab, a.nR, a.L, a.nA, a.chunkE, 1, 0, 256, sizeof(TE), sizeof(TE), true);
+  const EFLayout lay = ef_layout(a.ntab, a.nRs, a.L, a.nA, a.chunkE, 1, 0, 256, sizeof(TE), sizeof(TE), true);
   TE *tabE = (TE *)(sm + lay.tabE);
   int16_t *s_an = (int16_t *)(sm + lay.an);
   int16_t *s_aiy = (int16_t *)(sm + lay.aiy);
@@ -517,6 +544,9 @@ inline EFArgs make_args(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const do
     default: a.tabE = ctx->d_tabF; a.tabG = ctx->d_tabF; break;
   }
   a.ntab = ctx->ntab; a.nR = ctx->nR; a.L = ctx->L; a.pl = ctx->pl; a.pr = ctx->pr; a.tp = ctx->tp;
+  a.nRs = ctx->learned ? ctx->mlpC : ctx->nR;
+  a.Rext = ctx->learned ? ctx->d_Rext : nullptr;
+  a.GR = nullptr;
   a.an = ctx->d_an; a.aiy = ctx->d_aiy; a.amu = ctx->d_amu;
   a.nA = ctx->nA; a.nspecies = ctx->nspecies;
   a.srec = ctx->d_srec; a.sc = ctx->d_sc; a.slen = ctx->slen;

@@ -62,18 +62,21 @@ int kernels_prepare(ace_ctx *ctx) {
   // private adjoint bins (phase 2); smaller regions raise occupancy
   const int region = ctx->region_kb * 1024;
   // column-parallel 1p basis: (L+1) threads per neighbour
-  const int slabE = (ctx->nR + 2 * size_y(ctx->L)) * sE;
-  const int slabG = (2 * ctx->nR + 8 * size_y(ctx->L)) * sG;
+  const int nRs = ctx->learned ? ctx->mlpC : ctx->nR;
+  const bool radj = ctx->learned;
+  const int slabE = (nRs + 2 * size_y(ctx->L)) * sE;
+  const int slabG = (2 * nRs + 8 * size_y(ctx->L) + (radj ? nRs : 0)) * sG;
   const int lanes = NT / (ctx->L + 1);
   ctx->chunkE = std::max(1, std::min(lanes, region / slabE));
   ctx->chunkG = std::max(1, std::min(lanes, region / slabG));
   ctx->npriv = std::max(1, std::min(ctx->nA, region / (NT * 2 * sG)));
-  EFLayout lay = ef_layout(ctx->ntab, ctx->nR, ctx->L, ctx->nA, ctx->chunkE, ctx->chunkG, ctx->npriv, NT, sE, sG, same);
+  EFLayout lay = ef_layout(ctx->ntab, nRs, ctx->L, ctx->nA, ctx->chunkE, ctx->chunkG, ctx->npriv, NT, sE, sG, same,
+                           radj);
   while (lay.total > (size_t)ctx->smem_optin && (ctx->chunkE > 1 || ctx->chunkG > 1 || ctx->npriv > 1)) {
     ctx->chunkE = std::max(1, ctx->chunkE / 2);
     ctx->chunkG = std::max(1, ctx->chunkG / 2);
     ctx->npriv = std::max(1, ctx->npriv / 2);
-    lay = ef_layout(ctx->ntab, ctx->nR, ctx->L, ctx->nA, ctx->chunkE, ctx->chunkG, ctx->npriv, NT, sE, sG, same);
+    lay = ef_layout(ctx->ntab, nRs, ctx->L, ctx->nA, ctx->chunkE, ctx->chunkG, ctx->npriv, NT, sE, sG, same, radj);
   }
   if (lay.total > (size_t)ctx->smem_optin) {
     ctx->err = "spec too large for shared memory";
@@ -92,7 +95,7 @@ int kernels_prepare(ace_ctx *ctx) {
   ctx->grid = ctx->nsm * std::max(occ, 1);
   // basis path (AA materialisation)
   ctx->aa_chunk = std::max(1, std::min(256 / (ctx->L + 1), (32 * 1024) / slabE));
-  EFLayout la = ef_layout(ctx->ntab, ctx->nR, ctx->L, ctx->nA, ctx->aa_chunk, 1, 0, 256, sE, sE, true);
+  EFLayout la = ef_layout(ctx->ntab, nRs, ctx->L, ctx->nA, ctx->aa_chunk, 1, 0, 256, sE, sE, true);
   ctx->aa_smem = la.total;
   void *fa = aa_func(ctx);
   if (cudaFuncSetAttribute(fa, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)la.total) != cudaSuccess) {
@@ -108,6 +111,10 @@ int kernels_prepare(ace_ctx *ctx) {
 int launch_energy_forces(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const double *rr, const int32_t *sp,
                          double *E, double *G, cudaStream_t st, const void *ic, double c0) {
   if (nEnv == 0) return ACE_OK;
+  if (ctx->learned) {
+    int rc = learned_radials(ctx, nEnv, off, rr, sp, st);
+    if (rc) return rc;
+  }
   EFArgs a = make_args(ctx, nEnv, off, rr, sp, E, G);
   if (ic) { a.ic = ic; a.c0 = c0; }
   void *f = ef_func(ctx, G != nullptr);
@@ -127,10 +134,30 @@ static int ensure_scratch(ace_ctx *ctx, size_t bytes) {
   return ACE_OK;
 }
 
+int launch_radial_adjoint(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const double *rr, const int32_t *sp,
+                          double *E, double *G, float *GR, cudaStream_t st) {
+  if (nEnv == 0) return ACE_OK;
+  int rc = learned_radials(ctx, nEnv, off, rr, sp, st);
+  if (rc) return rc;
+  EFArgs a = make_args(ctx, nEnv, off, rr, sp, E, G);
+  a.GR = GR;
+  void *f = ef_func(ctx, true);
+  const int grid = (int)std::min<int64_t>(nEnv, ctx->grid);
+  void *args[] = {&a};
+  cudaError_t e = cudaLaunchKernel(f, dim3(grid), dim3(NT), args, ctx->smem, st);
+  ctx->launches += 1;
+  if (e != cudaSuccess) { ctx->err = cudaGetErrorString(e); return ACE_ERR_CUDA; }
+  return ACE_OK;
+}
+
 int launch_basis(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const double *rr, const int32_t *sp,
                  double *B, double *dB, cudaStream_t st) {
   (void)dB;  // the derivative is produced by launch_dbasis
   if (nEnv == 0) return ACE_OK;
+  if (ctx->learned) {
+    int rc = learned_radials(ctx, nEnv, off, rr, sp, st);
+    if (rc) return rc;
+  }
   const bool f32 = (ctx->prec == ACE_PREC_FP32 || ctx->prec == ACE_PREC_FP32_BF16X3);
   const size_t ts = f32 ? 4 : 8;
   int64_t per = std::max<int64_t>(1, (int64_t)((512ull << 20) / (ctx->nAA * ts)));

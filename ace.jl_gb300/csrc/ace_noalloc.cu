@@ -80,6 +80,7 @@ extern "C" int ace_basis_noalloc(ace_ctx *ctx, int64_t nEnv, const int64_t *offs
   using namespace ace;
   if (!ctx) return ACE_ERR_INVALID;
   if (nEnv < 0 || !offsets || !rr || !B) return fail(ctx, ACE_ERR_INVALID, "NULL or negative argument");
+  if (ctx->learned) return fail(ctx, ACE_ERR_UNSUPPORTED, "the learned radial form allocates its radial buffer");
   if (ctx->nB == 0) return fail(ctx, ACE_ERR_INVALID, "spec has no U");
   if (ctx->nspecies > 1 && !species) return fail(ctx, ACE_ERR_INVALID, "species required for a multi-species spec");
   const bool f32 = (ctx->prec == ACE_PREC_FP32 || ctx->prec == ACE_PREC_FP32_BF16X3);

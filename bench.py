@@ -11,7 +11,14 @@ with inputs resident in HBM (L2 flushed between steps); `e2e` times the
 C-ABI call with pinned host buffers (host->device copy of positions,
 device->host copy of energies and gradients inside the timed region).
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+`--workload` selects one of the larger measured configurations instead:
+``ord5_deg16`` (order 5, degree 16, L 16; 500,000 environments x 30
+neighbours) and ``ord4_deg10_4sp`` (4 species, order 4, degree 10, L 10;
+250,000 environments whose neighbour counts are 60 % U{40..80} and 40 %
+U{8..20}, species uniform).  On those the FP64 form is timed on a prefix of
+the batch (``fp64_envs``) to keep a step within seconds.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--workload NAME]
 """
 from __future__ import annotations
 
@@ -31,8 +38,18 @@ sys.path.insert(0, os.path.join(ROOT, "ace.jl_gb300"))
 METRIC = "env-evals/s (E+F) on 1 GB300: chosen form vs plain FP64 path at <=1e-6 rel err"
 UNIT = "env/s"
 CHOSEN = "fp32x2"
-WORKLOAD = dict(name="ace-invariant ord4 deg12 L12, 100k envs, J~U{20..60}",
-                maxorder=4, maxdeg=12, maxL=12, nenv=100_000, jlo=20, jhi=60, seed=2024)
+WORKLOADS = {
+    "ord4_deg12": dict(name="ace-invariant ord4 deg12 L12, 100k envs, J~U{20..60}",
+                       maxorder=4, maxdeg=12, maxL=12, nspecies=1, nenv=100_000, jlo=20, jhi=60, seed=2024,
+                       fp64_envs=None),
+    "ord5_deg16": dict(name="ace-invariant ord5 deg16 L16, 500k envs, J=30",
+                       maxorder=5, maxdeg=16, maxL=16, nspecies=1, nenv=500_000, jlo=30, jhi=30, seed=2024,
+                       fp64_envs=20_000),
+    "ord4_deg10_4sp": dict(name="ace-invariant 4 species ord4 deg10 L10, 250k envs, J 60% U{40..80} / 40% U{8..20}",
+                           maxorder=4, maxdeg=10, maxL=10, nspecies=4, nenv=250_000, jlo=8, jhi=80, seed=2024,
+                           bimodal=(0.6, (40, 80), (8, 20)), fp64_envs=20_000),
+}
+WORKLOAD = WORKLOADS["ord4_deg12"]
 
 
 def dist_info():
@@ -45,9 +62,11 @@ def dist_info():
 def build_workload(nenv=None):
     from ace_gb300.configs import random_batch
     from ace_gb300.spec import random_coefficients, symmetric_basis
-    spec = symmetric_basis(WORKLOAD["maxorder"], WORKLOAD["maxdeg"], maxL=WORKLOAD["maxL"])
-    c = random_coefficients(spec, seed=WORKLOAD["seed"])
-    b = random_batch(nenv or WORKLOAD["nenv"], WORKLOAD["jlo"], WORKLOAD["jhi"], seed=WORKLOAD["seed"])
+    W = WORKLOAD
+    spec = symmetric_basis(W["maxorder"], W["maxdeg"], maxL=W["maxL"], nspecies=W["nspecies"])
+    c = random_coefficients(spec, seed=W["seed"])
+    b = random_batch(nenv or W["nenv"], W["jlo"], W["jhi"], nspecies=W["nspecies"], seed=W["seed"],
+                     bimodal=W.get("bimodal"))
     return spec, c, b
 
 
@@ -156,8 +175,9 @@ def cpu_baseline(spec, c, b, threads=0, target_s=8.0):
     n = 256
     while True:
         off = b.offsets[:n + 1]
+        sp = None if b.species is None else b.species[:off[-1]]
         t0 = time.perf_counter()
-        orc.energy_forces(off, b.rr[:off[-1]], nthreads=nthreads)
+        orc.energy_forces(off, b.rr[:off[-1]], sp, nthreads=nthreads)
         dt = time.perf_counter() - t0
         if dt >= target_s or n >= b.nenv:
             break
@@ -177,17 +197,20 @@ def run_reference(args):
     orc = oracle.Oracle(spec, c)
     nthreads = os.cpu_count()
     # each step: a bounded sample of the workload (a contiguous block of environments)
-    n = 2048
+    n = 256
     off = b.offsets[:n + 1]
-    t0 = time.perf_counter(); orc.energy_forces(off, b.rr[:off[-1]], nthreads=nthreads); dt = time.perf_counter() - t0
+    sp = None if b.species is None else b.species[:off[-1]]
+    t0 = time.perf_counter(); orc.energy_forces(off, b.rr[:off[-1]], sp, nthreads=nthreads)
+    dt = time.perf_counter() - t0
     n = int(min(b.nenv, max(256, n * 6.0 / max(dt, 1e-3))))
     times = []
     for step in range(args.warmup + args.steps):
         e0 = (step * n) % (b.nenv - n + 1)
         off = b.offsets[e0:e0 + n + 1] - b.offsets[e0]
         rr = b.rr[b.offsets[e0]:b.offsets[e0 + n]]
+        sp = None if b.species is None else b.species[b.offsets[e0]:b.offsets[e0 + n]]
         t0 = time.perf_counter()
-        orc.energy_forces(off, rr, nthreads=nthreads)
+        orc.energy_forces(off, rr, sp, nthreads=nthreads)
         if step >= args.warmup:
             times.append(time.perf_counter() - t0)
     tot = sum(times)
@@ -212,7 +235,10 @@ def main():
     ap.add_argument("--nenv", type=int, default=None, help="smaller workload (profiling only)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--workload", default="ord4_deg12", choices=sorted(WORKLOADS))
     args = ap.parse_args()
+    global WORKLOAD
+    WORKLOAD = WORKLOADS[args.workload]
     if args.impl == "reference":
         return run_reference(args)
 
@@ -234,14 +260,16 @@ def main():
     dev = torch.device("cuda", local)
     off_d = torch.from_numpy(b.offsets).to(dev)
     rr_d = torch.from_numpy(b.rr).to(dev)
+    sp_d = None if b.species is None else torch.from_numpy(b.species).to(dev)
     E_d = torch.empty(nenv, dtype=torch.float64, device=dev)
     G_d = torch.empty_like(rr_d)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # 256 MB > L2
     stream = torch.cuda.current_stream(dev)
 
-    def timed(ctx, steps, warmup):
+    def timed(ctx, steps, warmup, n=nenv):
+        o_d, e_d = off_d[:n + 1], E_d[:n]
         for _ in range(warmup):
-            ctx.energy_forces_device(off_d, rr_d, None, E_d, G_d, stream=stream.cuda_stream, sync=False)
+            ctx.energy_forces_device(o_d, rr_d, sp_d, e_d, G_d, stream=stream.cuda_stream, sync=False)
         torch.cuda.synchronize()
         if world > 1:
             dist.barrier()
@@ -252,7 +280,7 @@ def main():
             flush.zero_()
             s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             s.record(stream)
-            ctx.energy_forces_device(off_d, rr_d, None, E_d, G_d, stream=stream.cuda_stream, sync=False)
+            ctx.energy_forces_device(o_d, rr_d, sp_d, e_d, G_d, stream=stream.cuda_stream, sync=False)
             e.record(stream)
             e.synchronize()
             tot += s.elapsed_time(e) / 1e3
@@ -268,14 +296,17 @@ def main():
     ctx64 = Context(spec, "fp64", device=local)
     ctx64.set_params(c)
     k64 = max(1, min(args.steps, 3))
-    t64, _ = timed(ctx64, k64, min(args.warmup, 1))
-    E64 = E_d.cpu().numpy().copy(); G64 = G_d.cpu().numpy().copy()
+    n64 = min(nenv, WORKLOAD["fp64_envs"] or nenv)
+    t64, _ = timed(ctx64, k64, min(args.warmup, 1), n64)
+    m64 = int(b.offsets[n64])
+    E64 = E_d[:n64].cpu().numpy().copy(); G64 = G_d[:m64].cpu().numpy().copy()
     scale = np.maximum(np.abs(E64), np.sqrt(np.mean(E64 ** 2)))
 
     def errors():
-        E = E_d.cpu().numpy(); G = G_d.cpu().numpy()
+        E = E_d[:n64].cpu().numpy(); G = G_d[:m64].cpu().numpy()
         return {"E_rel_max_vs_fp64": float(np.max(np.abs(E - E64) / scale)),
-                "F_rel_max_vs_fp64": float(np.max(np.abs(G - G64)) / np.max(np.abs(G64)))}
+                "F_rel_max_vs_fp64": float(np.max(np.abs(G - G64)) / np.max(np.abs(G64))),
+                "envs_compared": n64}
     # plain FP32 (fast, not within the 1e-6 bar)
     ctx32 = Context(spec, "fp32", device=local)
     ctx32.set_params(c)
@@ -285,7 +316,7 @@ def main():
     # launch configuration picked by the autotuner on this batch
     ctx = Context(spec, CHOSEN, device=local)
     ctx.set_params(c)
-    tuned = ctx.autotune(off_d, rr_d, None, E_d, G_d, reps=1, stream=stream.cuda_stream)
+    tuned = ctx.autotune(off_d, rr_d, sp_d, E_d, G_d, reps=1, stream=stream.cuda_stream)
     torch.cuda.synchronize()
     with Clocks(local) as clk:
         t32, launches = timed(ctx, args.steps, args.warmup)
@@ -299,6 +330,7 @@ def main():
     if not args.no_e2e:
         off_h = torch.from_numpy(b.offsets).pin_memory().numpy()
         rr_h = torch.from_numpy(b.rr).pin_memory().numpy()
+        sp_h = None if b.species is None else torch.from_numpy(b.species).pin_memory().numpy()
         E_h = torch.empty(nenv, dtype=torch.float64).pin_memory().numpy()
         G_h = torch.empty((nnbr, 3), dtype=torch.float64).pin_memory().numpy()
         import ctypes as C
@@ -306,7 +338,8 @@ def main():
         lib = ctx.lib
 
         def call():
-            rc = lib.ace_energy_forces(ctx.h, nenv, _ptr(off_h), _ptr(rr_h), None, _ptr(E_h), _ptr(G_h), 0, None)
+            rc = lib.ace_energy_forces(ctx.h, nenv, _ptr(off_h), _ptr(rr_h), _ptr(sp_h), _ptr(E_h), _ptr(G_h), 0,
+                                       None)
             assert rc == 0, lib.ace_last_error_string(ctx.h)
         for _ in range(args.warmup):
             call()
@@ -321,7 +354,7 @@ def main():
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             tt = float(t.item())
         e2e = {"value": nenv * args.steps * world / tt, "unit": UNIT,
-               "h2d_bytes_per_step": int(off_h.nbytes + rr_h.nbytes),
+               "h2d_bytes_per_step": int(off_h.nbytes + rr_h.nbytes + (0 if sp_h is None else sp_h.nbytes)),
                "d2h_bytes_per_step": int(E_h.nbytes + G_h.nbytes)}
 
     if rank != 0:
@@ -334,7 +367,7 @@ def main():
     achieved = fl / (t32 / args.steps) / 1e12
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "ef_kernel_fp32x2_traffic.json")
-    if os.path.exists(tpath):
+    if os.path.exists(tpath) and args.workload == "ord4_deg12":
         tr = json.load(open(tpath))
         traffic = tr["dram_bytes_per_env"] * nenv
     roof = {"bound": "fp32", "achieved": achieved, "peak": peaks["fp32_tflops"], "unit": "TFLOP/s",
@@ -350,7 +383,7 @@ def main():
                        "form": "fp32x2: Rn, Ylm, A and the AA energy in double-float (FP32 pairs), adjoint and forces in FP32",
                        "l2": "flushed (256 MB write) between timed steps", "parallelism": f"replicas x{world}",
                        "autotuned": {"region_kb": tuned % 1000, "schedule": "items" if tuned >= 1000 else "trie"}},
-            "forms": {"fp64": {"value": nenv * k64 * world / t64, "ms_per_step": 1e3 * t64 / k64},
+            "forms": {"fp64": {"value": n64 * k64 * world / t64, "ms_per_step": 1e3 * t64 / k64, "envs": n64},
                       "fp32": {"value": nenv * args.steps * world / t32p, "ms_per_step": 1e3 * t32p / args.steps,
                                "error": err32},
                       "fp32x2": {"value": value, "ms_per_step": ms, "error": err}},

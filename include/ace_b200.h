@@ -172,6 +172,64 @@ int ace_autotune(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, const doubl
                  const int32_t *species, double *E, double *dEdrr, int32_t reps, void *stream,
                  int32_t *choice);
 
+/* ---------------------------------------------------------------------
+   Learned radial form.  No counterpart in the reference: it replaces the
+   radial basis x species one-hot of the 1p basis (src/b1pcomponents/Rn.jl:
+   17-29 times src/discrete1pbasis.jl:78-123) by K channels per l computed
+   by a small MLP of (transformed distance, neighbour species):
+
+     t = ((1 + r0)/(1 + r))^p and the envelope fe(t) of the spec's radial basis
+     x = 2 (t - tl)/(tmax - tl) - 1,  f = [T_0(x) .. T_{Q-1}(x), onehot(s)]
+     h1 = silu(W1 f + b1), h2 = silu(W2 h1 + b2)   (H = 64)
+     R_{k + K l}(r, s) = fe(t) (W3 h2 + b3)_{k + K l}
+
+   params = [W1 (H x (Q+S)) | b1 (H) | W2 (H x H) | b2 (H) | W3 (C x H) | b3 (C)],
+   C = K (L + 1), row-major FP32.  The context's spec must be single-species
+   with nR = K; A entry (n, l, m) then reads channel (n - 1) + K l.  After
+   ace_set_radial_mlp the context's ace_energy_forces / ace_energy /
+   ace_basis evaluate the learned form (species index the MLP's one-hot);
+   ace_basis with dB, ace_adjoint_eval_d and ace_basis_noalloc return
+   ACE_ERR_UNSUPPORTED.  The training entry points below take device
+   pointers only and run asynchronously on `stream`. */
+typedef struct ace_radial_mlp {
+  int32_t version;  /* 1 */
+  int32_t K, Q, nspecies, H;
+  double tmax;      /* feature scale: transform value mapped to x = +1 */
+  const float *params;
+  int64_t nparams;
+} ace_radial_mlp;
+
+/* Switch the context to the learned form (first call) or replace the
+   parameters (later calls, same shape). */
+int ace_set_radial_mlp(ace_ctx *ctx, const ace_radial_mlp *mlp);
+
+/* Device pointer to the context's parameter array (updated in place by
+   training) and its length. */
+int ace_radial_mlp_params(ace_ctx *ctx, float **d_params, int64_t *nparams);
+
+/* Copy the parameters out (host memory, or device memory with
+   ACE_OUTPUTS_ON_DEVICE); synchronous. */
+int ace_radial_mlp_get_params(ace_ctx *ctx, float *params, int32_t flags);
+
+/* R[j][c] = R_c(r_j) and R[j][C + c] = dR_c/dr for nNbr neighbours (device). */
+int ace_radial_mlp_forward(ace_ctx *ctx, int64_t nNbr, const double *rr, const int32_t *species, float *R,
+                           void *stream);
+
+/* gparams += sum_j wj[j] sum_c gR[j][c] dR_c(r_j)/dparams (device; wj may be
+   NULL for weights 1). */
+int ace_radial_mlp_backward(ace_ctx *ctx, int64_t nNbr, const double *rr, const int32_t *species,
+                            const float *gR, const float *wj, float *gparams, void *stream);
+
+/* Energies (and dE/drr when dEdrr is not NULL) of the learned form, and
+   GR[j][c] = dE/dR_c(r_j): the adjoint of src/evaluator.jl:161-200 stopped
+   at the radial values (device pointers). */
+int ace_energy_radial_adjoint(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, const double *rr,
+                              const int32_t *species, double *E, double *dEdrr, float *GR, void *stream);
+
+/* One Adam step on n parameters (device): m, v moments; step >= 1. */
+int ace_adam_step(int64_t n, float *w, const float *g, float *m, float *v, float lr, float beta1, float beta2,
+                  float eps, int32_t step, void *stream);
+
 /* Wait for the context's outstanding work; returns the kernels' status. */
 int ace_sync(ace_ctx *ctx);
 

@@ -304,12 +304,14 @@ static void work_free(work_t *w) {
 static inline int species_of(const int32_t *species, int64_t j) { return species ? species[j] : 0; }
 
 /* A = sum_j phi(X_j) through the evaluate path (product_1pbasis.jl:99-134) */
-static void eval_A(const oracle_spec *s, work_t *w, const double *rr, const int32_t *sp, int64_t J) {
+static void eval_A(const oracle_spec *s, work_t *w, const double *rr, const int32_t *sp, int64_t J,
+                   int64_t o) {
   for (int i = 0; i < s->nA; ++i) { w->A[i].re = 0.0; w->A[i].im = 0.0; }
   for (int64_t j = 0; j < J; ++j) {
     const double *x = rr + 3 * j;
     double r = sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
-    radial_eval(s, transform_t(s, r), w->R);
+    if (s->Rext) memcpy(w->R, s->Rext + (o + j) * s->nR, sizeof(double) * s->nR);
+    else radial_eval(s, transform_t(s, r), w->R);
     spher S = cart2spher(x);
     alp_eval(s->L, w->alpA, w->alpB, &S, w->P);
     cylm(s->L, &S, w->P, w->Y);
@@ -324,15 +326,22 @@ static void eval_A(const oracle_spec *s, work_t *w, const double *rr, const int3
 
 /* A and materialised dA[i, j] through the evaluate_ed path
    (product_1pbasis.jl:169-244) */
-static void eval_A_dA(const oracle_spec *s, work_t *w, const double *rr, const int32_t *sp, int64_t J) {
+static void eval_A_dA(const oracle_spec *s, work_t *w, const double *rr, const int32_t *sp, int64_t J,
+                      int64_t o) {
   for (int i = 0; i < s->nA; ++i) { w->A[i].re = 0.0; w->A[i].im = 0.0; }
   for (int64_t j = 0; j < J; ++j) {
     const double *x = rr + 3 * j;
     double r = sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
     double t = transform_t(s, r);
-    radial_eval_ed(s, t, w->R, w->dR);
     /* dR_n = P_n'(t) * (t'(r) * rr/r) */
     double dt = transform_dt(s, r);
+    if (s->Rext) {
+      memcpy(w->R, s->Rext + (o + j) * s->nR, sizeof(double) * s->nR);
+      memcpy(w->dR, s->dRext + (o + j) * s->nR, sizeof(double) * s->nR);
+      dt = 1.0;  /* dRext is already dR/dr */
+    } else {
+      radial_eval_ed(s, t, w->R, w->dR);
+    }
     double g[3] = {dt * (x[0] / r), dt * (x[1] / r), dt * (x[2] / r)};
     spher S = cart2spher(x);
     alp_eval_ed(s->L, w->alpA, w->alpB, &S, w->P, w->dP);
@@ -409,7 +418,7 @@ int oracle_energy(const oracle_spec *s, int64_t nEnv, const int64_t *offsets,
 #endif
       for (int64_t e = 0; e < nEnv; ++e) {
         int64_t o = offsets[e], J = offsets[e + 1] - offsets[e];
-        eval_A(s, &w, rr + 3 * o, species ? species + o : NULL, J);
+        eval_A(s, &w, rr + 3 * o, species ? species + o : NULL, J, o);
         E[e] = energy_from_A(s, w.A);
       }
     }
@@ -420,8 +429,8 @@ int oracle_energy(const oracle_spec *s, int64_t nEnv, const int64_t *offsets,
 
 /* _rrule_evaluate (evaluator.jl:161-200): G[3*j + a] = dE/drr_j[a] */
 static void grad_env(const oracle_spec *s, work_t *w, const double *rr, const int32_t *sp,
-                     int64_t J, double *G) {
-  eval_A_dA(s, w, rr, sp, J);
+                     int64_t J, int64_t o, double *G) {
+  eval_A_dA(s, w, rr, sp, J, o);
   for (int i = 0; i < s->nA; ++i) { w->dAco[i].re = 0.0; w->dAco[i].im = 0.0; }
   int64_t i0 = (s->nAA > 0 && s->orders[0] == 0) ? 1 : 0;
   for (int64_t iAA = i0; iAA < s->nAA; ++iAA) {
@@ -467,7 +476,7 @@ int oracle_grad_config(const oracle_spec *s, int64_t nEnv, const int64_t *offset
 #endif
       for (int64_t e = 0; e < nEnv; ++e) {
         int64_t o = offsets[e], J = offsets[e + 1] - offsets[e];
-        grad_env(s, &w, rr + 3 * o, species ? species + o : NULL, J, G + 3 * o);
+        grad_env(s, &w, rr + 3 * o, species ? species + o : NULL, J, o, G + 3 * o);
       }
     }
     work_free(&w);
@@ -494,9 +503,9 @@ int oracle_energy_forces(const oracle_spec *s, int64_t nEnv, const int64_t *offs
       for (int64_t e = 0; e < nEnv; ++e) {
         int64_t o = offsets[e], J = offsets[e + 1] - offsets[e];
         const int32_t *sp = species ? species + o : NULL;
-        eval_A(s, &w, rr + 3 * o, sp, J);
+        eval_A(s, &w, rr + 3 * o, sp, J, o);
         E[e] = energy_from_A(s, w.A);
-        grad_env(s, &w, rr + 3 * o, sp, J, G + 3 * o);
+        grad_env(s, &w, rr + 3 * o, sp, J, o, G + 3 * o);
       }
     }
     work_free(&w);
@@ -520,7 +529,7 @@ int oracle_A(const oracle_spec *s, int64_t nEnv, const int64_t *offsets, const d
 #endif
       for (int64_t e = 0; e < nEnv; ++e) {
         int64_t o = offsets[e], J = offsets[e + 1] - offsets[e];
-        eval_A(s, &w, rr + 3 * o, species ? species + o : NULL, J);
+        eval_A(s, &w, rr + 3 * o, species ? species + o : NULL, J, o);
         memcpy(Aout + 2 * (size_t)e * s->nA, w.A, sizeof(cplx) * s->nA);
       }
     }
@@ -546,7 +555,7 @@ int oracle_basis(const oracle_spec *s, int64_t nEnv, const int64_t *offsets, con
 #endif
       for (int64_t e = 0; e < nEnv; ++e) {
         int64_t o = offsets[e], J = offsets[e + 1] - offsets[e];
-        eval_A(s, &w, rr + 3 * o, species ? species + o : NULL, J);
+        eval_A(s, &w, rr + 3 * o, species ? species + o : NULL, J, o);
         /* PIBasis evaluate! (pibasis.jl:265-275) */
         for (int64_t iAA = 0; iAA < s->nAA; ++iAA) {
           const int32_t *v = s->iAA2iA + iAA * s->maxord;
@@ -588,7 +597,7 @@ int oracle_basis_d(const oracle_spec *s, int64_t nEnv, const int64_t *offsets, c
 #endif
       for (int64_t e = 0; e < nEnv; ++e) {
         int64_t o = offsets[e], J = offsets[e + 1] - offsets[e];
-        eval_A_dA(s, &w, rr + 3 * o, species ? species + o : NULL, J);
+        eval_A_dA(s, &w, rr + 3 * o, species ? species + o : NULL, J, o);
         int64_t i0 = 0;
         if (s->nAA > 0 && s->orders[0] == 0) {
           w.AA[0] = 1.0;
@@ -640,6 +649,58 @@ int oracle_basis_d(const oracle_spec *s, int64_t nEnv, const int64_t *offsets, c
 /* ------------------------------------------------- component access (tests) */
 
 /* Y (and dY when dY != NULL) at one point, through cYlm! or cYlm_ed! */
+/* dE/dR_n(r_j): the adjoint dAco of grad_env contracted with Y instead of dA
+   (the chain rule of src/evaluator.jl:187-192 stopped at the radial values) */
+int oracle_radial_adjoint(const oracle_spec *s, int64_t nEnv, const int64_t *offsets,
+                          const double *rr, const int32_t *species, double *E, double *GR,
+                          int nthreads) {
+  int err = 0;
+  int64_t mJ = max_J(nEnv, offsets);
+#ifdef _OPENMP
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel num_threads(nthreads) reduction(| : err)
+#endif
+  {
+    work_t w;
+    if (work_init(&w, s, (int)mJ, 1, 0) != 0) err |= 1;
+    else {
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 4)
+#endif
+      for (int64_t e = 0; e < nEnv; ++e) {
+        int64_t o = offsets[e], J = offsets[e + 1] - offsets[e];
+        const int32_t *sp = species ? species + o : NULL;
+        eval_A(s, &w, rr + 3 * o, sp, J, o);
+        E[e] = energy_from_A(s, w.A);
+        for (int i = 0; i < s->nA; ++i) { w.dAco[i].re = 0.0; w.dAco[i].im = 0.0; }
+        int64_t i0 = (s->nAA > 0 && s->orders[0] == 0) ? 1 : 0;
+        for (int64_t iAA = i0; iAA < s->nAA; ++iAA) {
+          aa_local_adjoints(s, w.A, iAA, w.dAAdA);
+          const int32_t *v = s->iAA2iA + iAA * s->maxord;
+          double c = s->ctilde[iAA];
+          for (int t = 0; t < s->orders[iAA]; ++t)
+            w.dAco[v[t]] = cadd(w.dAco[v[t]], crmul(w.dAAdA[t], c));
+        }
+        for (int64_t j = 0; j < J; ++j) {
+          const double *x = rr + 3 * (o + j);
+          spher S = cart2spher(x);
+          alp_eval(s->L, w.alpA, w.alpB, &S, w.P);
+          cylm(s->L, &S, w.P, w.Y);
+          double *g = GR + (o + j) * s->nR;
+          for (int n = 0; n < s->nR; ++n) g[n] = 0.0;
+          int mu = species_of(sp, j);
+          for (int i = 0; i < s->nA; ++i) {
+            if (s->a_mu && s->a_mu[i] != mu) continue;
+            g[s->a_n[i]] += cmul(w.dAco[i], w.Y[s->a_iy[i]]).re;
+          }
+        }
+      }
+    }
+    work_free(&w);
+  }
+  return err ? -1 : 0;
+}
+
 int oracle_sh(int L, const double *x, double *Y /* (L+1)^2 x 2 */, double *dY /* (L+1)^2 x 3 x 2 */) {
   int szP = (L + 1) * (L + 2) / 2;
   double *A = malloc(sizeof(double) * szP), *B = malloc(sizeof(double) * szP);

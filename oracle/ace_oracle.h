@@ -34,6 +34,10 @@ typedef struct {
   const int64_t *U_indptr;
   const int32_t *U_indices;
   const double *U_data;
+  /* externally supplied radial channels (learned radial form): when non-NULL,
+     R_n(r_j) = Rext[j * nR + n] and dR_n/dr(r_j) = dRext[j * nR + n] for the
+     batch's neighbour j (absolute index) replace the polynomial radial basis */
+  const double *Rext, *dRext;
 } oracle_spec;
 
 int oracle_energy(const oracle_spec *s, int64_t nEnv, const int64_t *offsets,
@@ -49,6 +53,12 @@ int oracle_basis(const oracle_spec *s, int64_t nEnv, const int64_t *offsets, con
                  const int32_t *species, double *B, int nthreads);
 int oracle_basis_d(const oracle_spec *s, int64_t nEnv, const int64_t *offsets, const double *rr,
                    const int32_t *species, double *B, double *dB, int nthreads);
+
+/* dE/dR_n(r_j) = sum_{i: a_n[i] == n} Re(dAco_i Y_{a_iy[i]}(rhat_j)) for every
+   neighbour j and radial channel n (GR is nNbr x nR), and E */
+int oracle_radial_adjoint(const oracle_spec *s, int64_t nEnv, const int64_t *offsets,
+                          const double *rr, const int32_t *species, double *E, double *GR,
+                          int nthreads);
 
 int oracle_sh(int L, const double *x, double *Y, double *dY);
 int oracle_radial(const oracle_spec *s, int64_t n, const double *r, double *R, double *dR);

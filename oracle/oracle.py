@@ -44,6 +44,7 @@ class _Spec(C.Structure):
         ("nAA", C.c_int64), ("maxord", C.c_int), ("orders", C.c_void_p), ("iAA2iA", C.c_void_p),
         ("ctilde", C.c_void_p),
         ("nB", C.c_int64), ("U_indptr", C.c_void_p), ("U_indices", C.c_void_p), ("U_data", C.c_void_p),
+        ("Rext", C.c_void_p), ("dRext", C.c_void_p),
     ]
 
 
@@ -60,6 +61,8 @@ def _lib():
             f = getattr(_LIB, name)
             f.restype = C.c_int
             f.argtypes = [P, C.c_int64, P, P, P, P, P, C.c_int]
+        _LIB.oracle_radial_adjoint.restype = C.c_int
+        _LIB.oracle_radial_adjoint.argtypes = [P, C.c_int64, P, P, P, P, P, C.c_int]
         _LIB.oracle_sh.restype = C.c_int
         _LIB.oracle_sh.argtypes = [C.c_int, P, P, P]
         _LIB.oracle_radial.restype = C.c_int
@@ -72,8 +75,13 @@ def _p(a):
 
 
 class Oracle:
-    def __init__(self, spec, c=None, ctilde=None):
+    """With ``channels_per_l = K`` the model is the learned-radial form: the
+    radial value of A entry (n, l, m) is channel (n-1) + K*l of externally
+    supplied per-neighbour radials (``set_radial``), nR = K*(L+1)."""
+
+    def __init__(self, spec, c=None, ctilde=None, channels_per_l=None):
         self.spec = spec
+        self.K = channels_per_l
         if ctilde is None:
             if c is None:
                 c = np.zeros(spec.nB)
@@ -85,7 +93,8 @@ class Oracle:
         k["rB"] = np.ascontiguousarray(R.J.B, dtype=np.float64)
         k["rC"] = np.ascontiguousarray(R.J.C, dtype=np.float64)
         a = spec.aspec
-        k["a_n"] = np.ascontiguousarray(a.n - 1, dtype=np.int32)
+        an = a.n - 1 if channels_per_l is None else (a.n - 1) + channels_per_l * a.l
+        k["a_n"] = np.ascontiguousarray(an, dtype=np.int32)
         k["a_iy"] = np.ascontiguousarray(a.l * a.l + a.l + a.m, dtype=np.int32)
         k["a_mu"] = np.ascontiguousarray(a.mu, dtype=np.int32) if spec.nspecies > 1 else None
         k["orders"] = np.ascontiguousarray(spec.orders, dtype=np.int32)
@@ -97,7 +106,7 @@ class Oracle:
         k["U_indices"] = np.ascontiguousarray(U.indices, dtype=np.int32)
         k["U_data"] = np.ascontiguousarray(U.data, dtype=np.float64)
         s = _Spec()
-        s.nR = len(R.J.A)
+        s.nR = len(R.J.A) if channels_per_l is None else channels_per_l * (spec.Leff + 1)
         s.rA, s.rB, s.rC = _p(k["rA"]), _p(k["rB"]), _p(k["rC"])
         s.pl, s.pr, s.tl, s.tr = R.J.pl, R.J.pr, R.J.tl, R.J.tr
         s.tp, s.r0 = R.trans.p, R.trans.r0
@@ -109,6 +118,25 @@ class Oracle:
         s.nB = spec.nB
         s.U_indptr, s.U_indices, s.U_data = _p(k["U_indptr"]), _p(k["U_indices"]), _p(k["U_data"])
         self._s = s
+
+    def set_radial(self, R, dR=None):
+        """Per-neighbour radial channels (nNbr x nR) and their r-derivatives
+        for the next calls (learned-radial form)."""
+        assert self.K is not None
+        self._keep["Rext"] = np.ascontiguousarray(R, dtype=np.float64)
+        self._keep["dRext"] = np.ascontiguousarray(R * 0 if dR is None else dR, dtype=np.float64)
+        assert self._keep["Rext"].shape[1] == self._s.nR
+        self._s.Rext, self._s.dRext = _p(self._keep["Rext"]), _p(self._keep["dRext"])
+
+    def radial_adjoint(self, offsets, rr, species=None, nthreads=0):
+        """E and dE/dR_n(r_j) (nNbr x nR)."""
+        offsets, rr, sp = self._inputs(offsets, rr, species)
+        E = np.zeros(len(offsets) - 1)
+        GR = np.zeros((len(rr), self._s.nR))
+        rc = _lib().oracle_radial_adjoint(C.byref(self._s), len(offsets) - 1, _p(offsets), _p(rr), _p(sp),
+                                          _p(E), _p(GR), nthreads)
+        assert rc == 0
+        return E, GR
 
     def set_params(self, c):
         """``set_params!`` (src/linearmodel.jl:67-71): c~ = U^T c."""

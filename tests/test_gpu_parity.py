@@ -41,6 +41,10 @@ SPECS = {
     "cfg1": dict(maxorder=3, maxdeg=8, maxL=6),
     "cfg2": dict(maxorder=4, maxdeg=12, maxL=12),
     "ord5": dict(maxorder=5, maxdeg=10, maxL=10),
+    # order 5 / degree 16 / L 16: 1,310,316 AA functions, 55,420 B functions
+    "ord5_deg16": dict(maxorder=5, maxdeg=16, maxL=16),
+    # 4 species, order 4 / degree 10 / L 10: 1,830,429 AA functions
+    "ord4_deg10_4sp": dict(maxorder=4, maxdeg=10, maxL=10, nspecies=4),
 }
 _spec_cache = {}
 
@@ -296,3 +300,82 @@ def test_cuda_graph_capture(lib, oracle_mod):
     Eref, Gref = oracle_mod.Oracle(spec, c).energy_forces(b.offsets, rr2)
     assert energy_relerr(E.cpu().numpy(), Eref) <= 1e-12
     assert relerr(G.cpu().numpy(), Gref) <= 1e-10
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32", "fp32x2"])
+def test_order5_degree16(lib, oracle_mod, prec):
+    """The order-5 / degree-16 basis (J = 30) against the oracle."""
+    spec = get_spec("ord5_deg16")
+    c = random_coefficients(spec, seed=4)
+    b = random_batch(12, 30, 30, seed=21)
+    orc = oracle_mod.Oracle(spec, c)
+    Eref, Gref = orc.energy_forces(b.offsets, b.rr)
+    ctx = lib.Context(spec, prec)
+    ctx.set_params(c)
+    E, G = ctx.energy_forces(b.offsets, b.rr)
+    print(f"ord5_deg16 {prec}: E relerr {energy_relerr(E, Eref):.3g}  G relerr {relerr(G, Gref):.3g}")
+    assert energy_relerr(E, Eref) <= TOL[prec]["E"]
+    assert relerr(G, Gref) <= TOL[prec]["G"]
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32", "fp32x2"])
+def test_four_species_bimodal(lib, oracle_mod, prec):
+    """4 species, order 4 / degree 10, neighbour counts 60 % U{40..80} and
+    40 % U{8..20}, against the oracle."""
+    spec = get_spec("ord4_deg10_4sp")
+    c = random_coefficients(spec, seed=8)
+    b = random_batch(16, 8, 80, nspecies=4, seed=13, bimodal=(0.6, (40, 80), (8, 20)))
+    orc = oracle_mod.Oracle(spec, c)
+    Eref, Gref = orc.energy_forces(b.offsets, b.rr, b.species)
+    ctx = lib.Context(spec, prec)
+    ctx.set_params(c)
+    E, G = ctx.energy_forces(b.offsets, b.rr, b.species)
+    print(f"ord4_deg10_4sp {prec}: E relerr {energy_relerr(E, Eref):.3g}  G relerr {relerr(G, Gref):.3g}")
+    assert energy_relerr(E, Eref) <= TOL[prec]["E"]
+    assert relerr(G, Gref) <= TOL[prec]["G"]
+
+
+def _rotation(seed):
+    q, r = np.linalg.qr(np.random.default_rng(seed).standard_normal((3, 3)))
+    q = q * np.sign(np.diag(r))
+    if np.linalg.det(q) < 0:
+        q[:, 0] = -q[:, 0]
+    return q
+
+
+def test_full_size_order4_degree12(lib, oracle_mod):
+    """The full order-4 / degree-12 workload (100,000 environments, J in
+    U{20..60}): the chosen fp32x2 form against the FP64 form on every
+    environment, the FP64 form against the oracle on a sample, O(3)
+    invariance of the energies and covariance of the gradients under a
+    rotation and a reflection, and invariance under a permutation of each
+    environment's neighbours."""
+    spec = get_spec("cfg2")
+    c = random_coefficients(spec, seed=2024)
+    b = random_batch(100_000, 20, 60, seed=2024)
+    c64 = lib.Context(spec, "fp64"); c64.set_params(c)
+    cx2 = lib.Context(spec, "fp32x2"); cx2.set_params(c)
+    E64, G64 = c64.energy_forces(b.offsets, b.rr)
+    E, G = cx2.energy_forces(b.offsets, b.rr)
+    assert energy_relerr(E, E64) <= 1e-6
+    assert relerr(G, G64) <= 1e-4
+    # oracle on a sample of 300 environments spread over the batch
+    idx = np.random.default_rng(0).choice(b.nenv, 300, replace=False)
+    off = np.concatenate([[0], np.cumsum(np.diff(b.offsets)[idx])])
+    rr = np.concatenate([b.rr[b.offsets[e]:b.offsets[e + 1]] for e in idx])
+    Eo, Go = oracle_mod.Oracle(spec, c).energy_forces(off, rr)
+    assert energy_relerr(E64[idx], Eo) <= 1e-12
+    Gs = np.concatenate([G64[b.offsets[e]:b.offsets[e + 1]] for e in idx])
+    assert relerr(Gs, Go) <= 1e-10
+    # O(3): E(Q r) = E(r), G(Q r) = Q G(r)
+    for Q in (_rotation(1), -_rotation(2)):
+        Er, Gr = cx2.energy_forces(b.offsets, b.rr @ Q.T)
+        assert energy_relerr(Er, E) <= 1e-6
+        assert relerr(Gr, G @ Q.T) <= 1e-4
+    # permutation of the neighbours inside every environment
+    rng = np.random.default_rng(3)
+    perm = np.concatenate([b.offsets[e] + rng.permutation(b.offsets[e + 1] - b.offsets[e])
+                           for e in range(b.nenv)])
+    Ep, Gp = cx2.energy_forces(b.offsets, b.rr[perm])
+    assert energy_relerr(Ep, E) <= 1e-6
+    assert relerr(Gp, G[perm]) <= 1e-4
