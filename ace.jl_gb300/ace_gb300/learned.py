@@ -14,8 +14,9 @@ the teacher by distillation:
    and species.  The pretrained student is the method without the network:
    a species-blind radial basis of width K.
 2. ``fit_coefficients``: the student's basis coefficients c by ridge least
-   squares on teacher energies of seeded environments (the student basis B
-   is evaluated on the GPU).
+   squares on teacher energies of seeded environments and, optionally, on
+   the teacher's per-neighbour gradients (c enters both linearly; the
+   student basis B and its derivative dB are evaluated on the GPU).
 3. ``distill``: Adam on the MLP parameters against the teacher energies, with
    c re-fitted every few hundred steps.  The gradient is exact for the
    energy loss: dL/dR_c(r_j) comes from the energy kernel's adjoint
@@ -181,36 +182,52 @@ def pretrain_radial(ctx: Context, mlp: RadialMLP, spec: ACESpec, nsamples: int =
     return hist
 
 
-def _basis_device(ctx: Context, b: Batch):
-    return ctx.basis(b.offsets, b.rr, b.species)
-
-
-def fit_coefficients(ctx: Context, spec: ACESpec, b: Batch, E_target: np.ndarray, ridge: float = 1e-8):
-    """Ridge least squares for the student's basis coefficients c on target
-    energies: (B^T B + ridge tr(B^T B)/nB I) c = B^T E, with B the student
-    basis (nEnv x nB) from the GPU basis path."""
+def fit_coefficients(ctx: Context, spec: ACESpec, b: Batch, E_target: np.ndarray, ridge: float = 1e-8,
+                     forces=None):
+    """Ridge least squares for the student's basis coefficients c: energy
+    rows B c = E over the environments of b and, with forces = (bf, G, w),
+    gradient rows dB c = dE/drr over the neighbours of bf (weight w), each
+    block normalised by its target variance; the basis and its derivative
+    come from the GPU basis path (learned radials included)."""
     torch = _torch()
-    B = _basis_device(ctx, b)
     dev = torch.device("cuda", ctx.device)
-    Bt = torch.from_numpy(B).to(dev)
-    G = Bt.T @ Bt
-    lam = ridge * float(torch.trace(G)) / G.shape[0]
-    G += lam * torch.eye(G.shape[0], dtype=G.dtype, device=dev)
-    rhs = Bt.T @ torch.from_numpy(np.asarray(E_target, dtype=np.float64)).to(dev)
+    nB = spec.nB
+    B = torch.empty((b.nenv, nB), dtype=torch.float64, device=dev)
+    ctx.basis_to_device(b.offsets, b.rr, b.species, B)
+    Et = torch.from_numpy(np.asarray(E_target, dtype=np.float64)).to(dev)
+    se = float(Et.var()) or 1.0
+    G = (B.T @ B) / (b.nenv * se)
+    rhs = (B.T @ Et) / (b.nenv * se)
+    del B
+    if forces is not None:
+        bf, Gt, w = forces
+        Bf = torch.empty((bf.nenv, nB), dtype=torch.float64, device=dev)
+        dB = torch.empty((bf.nnbr, nB, 3), dtype=torch.float64, device=dev)
+        ctx.basis_to_device(bf.offsets, bf.rr, bf.species, Bf, dB)
+        D = dB.permute(0, 2, 1).reshape(-1, nB)
+        del dB, Bf
+        g = torch.from_numpy(np.ascontiguousarray(Gt, dtype=np.float64).reshape(-1)).to(dev)
+        sf = float((g * g).mean()) or 1.0
+        G += w * (D.T @ D) / (len(g) * sf)
+        rhs += w * (D.T @ g) / (len(g) * sf)
+        del D
+    lam = ridge * float(torch.trace(G)) / nB
+    G += lam * torch.eye(nB, dtype=G.dtype, device=dev)
     c = torch.linalg.solve(G, rhs)
     return c.cpu().numpy()
 
 
-def _sub(b: Batch, e0: int, e1: int) -> Batch:
+def sub_batch(b: Batch, e0: int, e1: int) -> Batch:
     o0, o1 = int(b.offsets[e0]), int(b.offsets[e1])
     return Batch(b.offsets[e0:e1 + 1] - o0, b.rr[o0:o1], None if b.species is None else b.species[o0:o1])
 
 
 def distill(ctx: Context, mlp: RadialMLP, spec: ACESpec, train: Batch, E_train: np.ndarray, c: np.ndarray,
             steps: int = 2000, batch_envs: int = 512, lr: float = 1e-3, refit_every: int = 500,
-            refit_envs: int = 20000, log=None):
+            refit_envs: int = 20000, forces=None, log=None):
     """Adam on the MLP parameters against teacher energies (c fixed between
-    ridge re-fits); returns (c, history)."""
+    ridge re-fits, which also use the teacher gradients `forces` when
+    given, see fit_coefficients); returns (c, history)."""
     torch = _torch()
     dev = torch.device("cuda", ctx.device)
     off_d = torch.from_numpy(train.offsets).to(dev)
@@ -228,7 +245,7 @@ def distill(ctx: Context, mlp: RadialMLP, spec: ACESpec, train: Batch, E_train: 
     ctx.set_params(c)
     hist = []
     rng = np.random.default_rng(11)
-    refit = _sub(train, 0, min(refit_envs, nEnv))
+    refit = sub_batch(train, 0, min(refit_envs, nEnv))
     for it in range(steps):
         e0 = int(rng.integers(0, max(1, nEnv - batch_envs)))
         e1 = min(nEnv, e0 + batch_envs)
@@ -253,10 +270,10 @@ def distill(ctx: Context, mlp: RadialMLP, spec: ACESpec, train: Batch, E_train: 
                 log(f"distill {it}: rel mse {loss:.3e}")
         if refit_every and (it + 1) % refit_every == 0 and it + 1 < steps:
             torch.cuda.synchronize()
-            c = fit_coefficients(ctx, spec, refit, E_train[:refit.nenv])
+            c = fit_coefficients(ctx, spec, refit, E_train[:refit.nenv], forces=forces)
             ctx.set_params(c)
     tr.params_to_host()
-    c = fit_coefficients(ctx, spec, refit, E_train[:refit.nenv])
+    c = fit_coefficients(ctx, spec, refit, E_train[:refit.nenv], forces=forces)
     ctx.set_params(c)
     return c, hist
 

@@ -211,6 +211,15 @@ class Context:
                                        _ptr(B), _ptr(dB), 0, None))
         return (B, dB) if grad else B
 
+    def basis_to_device(self, offsets, rr, species, B, dB=None):
+        """B (and dB) of host inputs into device tensors B (nEnv, nB) and dB
+        (nNbr, nB, 3)."""
+        offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+        rr = np.ascontiguousarray(rr, dtype=np.float64).reshape(-1, 3)
+        sp = None if species is None else np.ascontiguousarray(species, dtype=np.int32)
+        self._check(self.lib.ace_basis(self.h, len(offsets) - 1, _ptr(offsets), _ptr(rr), _ptr(sp),
+                                       _ptr(B), _ptr(dB), ACE_OUTPUTS_ON_DEVICE, None))
+
     def set_params_multi(self, c):
         """c: (nB, nprop) -- one column of coefficients per property."""
         c = np.asarray(c, dtype=np.float64)

@@ -77,8 +77,15 @@ __global__ void __launch_bounds__(256) daa_kernel(DArgs d) {
         const T x = T(a.rr[3 * j]), y = T(a.rr[3 * j + 1]), z = T(a.rr[3 * j + 2]);
         const Angles<T> g = angles(x, y, z);
         T *sl = slab + (size_t)cj * SG;
-        cpx<T> *Y = (cpx<T> *)(sl + 2 * a.nR);
+        cpx<T> *Y = (cpx<T> *)(sl + 2 * a.nRs);
         cpx<T> *dY = Y + nY;
+        if (a.Rext) {
+          const float *rx = a.Rext + (size_t)j * 2 * a.nRs;
+          for (int n = cm; n < a.nRs; n += LP1) {
+            sl[n] = T(rx[n]);
+            sl[a.nRs + n] = T(rx[a.nRs + n]);
+          }
+        }
         if (cm == 0) {
           int s = 0;
           if (a.nspecies > 1) {
@@ -89,7 +96,7 @@ __global__ void __launch_bounds__(256) daa_kernel(DArgs d) {
           const T ux = x / g.r, uy = y / g.r, uz = z / g.r;
           spos[4 * cj + 0] = ux; spos[4 * cj + 1] = uy; spos[4 * cj + 2] = uz;
           if (!DB) spos[4 * cj + 3] = T(d.w[3 * j]) * ux + T(d.w[3 * j + 1]) * uy + T(d.w[3 * j + 2]) * uz;
-          radial_eval<T, true>(tb, g.r, sl, sl + a.nR);
+          if (!a.Rext) radial_eval<T, true>(tb, g.r, sl, sl + a.nRs);
         }
         sh_col_grad<T>(tb, g, cm, Y, dY);
         if (!DB) {
@@ -110,9 +117,9 @@ __global__ void __launch_bounds__(256) daa_kernel(DArgs d) {
           for (int jj = 0; jj < nc; ++jj) {
             if (a.nspecies > 1 && ssp[jj] != mu) continue;
             const T *sl = slab + (size_t)jj * SG;
-            const cpx<T> *Y = (const cpx<T> *)(sl + 2 * a.nR);
+            const cpx<T> *Y = (const cpx<T> *)(sl + 2 * a.nRs);
             const cpx<T> g = (Y + nY)[3 * iy];
-            const T dRs = sl[a.nR + n] * spos[4 * jj + 3];
+            const T dRs = sl[a.nRs + n] * spos[4 * jj + 3];
             acc = cadd(acc, cadd(cscale(Y[iy], dRs), cscale(g, sl[n])));
           }
           Dw[i] = acc;
@@ -130,7 +137,7 @@ __global__ void __launch_bounds__(256) daa_kernel(DArgs d) {
           for (int t = ord - 1; t >= 0; --t) { adj[t] = cmul(adj[t], suf); suf = cmul(suf, AE[v[t]]); }
           for (int jj = 0; jj < nc; ++jj) {
             const T *sl = slab + (size_t)jj * SG;
-            const cpx<T> *Y = (const cpx<T> *)(sl + 2 * a.nR);
+            const cpx<T> *Y = (const cpx<T> *)(sl + 2 * a.nRs);
             const cpx<T> *dY = Y + nY;
             const int sp = ssp[jj];
             T g0 = T(0), g1 = T(0), g2 = T(0);
@@ -139,7 +146,7 @@ __global__ void __launch_bounds__(256) daa_kernel(DArgs d) {
               if (a.nspecies > 1 && s_amu[vv] != sp) continue;
               const int n = s_an[vv], iy = s_aiy[vv];
               const cpx<T> q = adj[t];
-              const T R = sl[n], dR = sl[a.nR + n];
+              const T R = sl[n], dR = sl[a.nRs + n];
               const T ry = q.re * Y[iy].re - q.im * Y[iy].im;
               const cpx<T> *g = dY + 3 * iy;
               g0 += dR * spos[4 * jj + 0] * ry + R * (q.re * g[0].re - q.im * g[0].im);
@@ -202,9 +209,14 @@ template <typename T, bool DB>
 static int run_daa(ace_ctx *ctx, int64_t nEnv, const int64_t *off_d, const int64_t *off_h, const double *rr,
                    const int32_t *sp, const double *w, double *out, cudaStream_t st) {
   const size_t ts = sizeof(T);
-  const int slabG = (2 * ctx->nR + 8 * size_y(ctx->L)) * (int)ts;
+  const int nRs = ctx->learned ? ctx->mlpC : ctx->nR;
+  const int slabG = (2 * nRs + 8 * size_y(ctx->L)) * (int)ts;
   int chunk = std::max(1, std::min(std::min(32, 256 / (ctx->L + 1)), (48 * 1024) / slabG));
-  EFLayout lay = ef_layout(ctx->ntab, ctx->nR, ctx->L, ctx->nA, chunk, chunk, 0, 256, (int)ts, (int)ts, true);
+  EFLayout lay = ef_layout(ctx->ntab, nRs, ctx->L, ctx->nA, chunk, chunk, 0, 256, (int)ts, (int)ts, true);
+  if (ctx->learned) {
+    int rc = learned_radials(ctx, nEnv, off_d, rr, sp, st);
+    if (rc) return rc;
+  }
   void *f = (void *)daa_kernel<T, DB>;
   if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lay.total) != cudaSuccess) {
     ctx->err = "cudaFuncSetAttribute failed";
@@ -258,7 +270,6 @@ static int run_daa(ace_ctx *ctx, int64_t nEnv, const int64_t *off_d, const int64
 int launch_dbasis(ace_ctx *ctx, int64_t nEnv, const int64_t *off_d, const int64_t *off_h, const double *rr,
                   const int32_t *sp, double *dB, cudaStream_t st) {
   if (nEnv == 0) return ACE_OK;
-  if (ctx->learned) { ctx->err = "basis derivatives are not available in the learned radial form"; return ACE_ERR_UNSUPPORTED; }
   if (ctx->prec == ACE_PREC_FP32 || ctx->prec == ACE_PREC_FP32_BF16X3)
     return run_daa<float, true>(ctx, nEnv, off_d, off_h, rr, sp, nullptr, dB, st);
   return run_daa<double, true>(ctx, nEnv, off_d, off_h, rr, sp, nullptr, dB, st);
@@ -267,7 +278,6 @@ int launch_dbasis(ace_ctx *ctx, int64_t nEnv, const int64_t *off_d, const int64_
 int launch_adjoint_eval_d(ace_ctx *ctx, int64_t nEnv, const int64_t *off_d, const int64_t *off_h,
                           const double *rr, const int32_t *sp, const double *w, double *out, cudaStream_t st) {
   if (nEnv == 0) return ACE_OK;
-  if (ctx->learned) { ctx->err = "basis derivatives are not available in the learned radial form"; return ACE_ERR_UNSUPPORTED; }
   if (ctx->prec == ACE_PREC_FP32 || ctx->prec == ACE_PREC_FP32_BF16X3)
     return run_daa<float, false>(ctx, nEnv, off_d, off_h, rr, sp, w, out, st);
   return run_daa<double, false>(ctx, nEnv, off_d, off_h, rr, sp, w, out, st);

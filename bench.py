@@ -11,7 +11,9 @@ with inputs resident in HBM (L2 flushed between steps); `e2e` times the
 C-ABI call with pinned host buffers (host->device copy of positions,
 device->host copy of energies and gradients inside the timed region).
 
-`--workload` selects one of the larger measured configurations instead:
+`--workload` selects one of the larger measured configurations instead
+(``learned_4sp`` distils and times the learned radial form on the 4-species
+model):
 ``ord5_deg16`` (order 5, degree 16, L 16; 500,000 environments x 30
 neighbours) and ``ord4_deg10_4sp`` (4 species, order 4, degree 10, L 10;
 250,000 environments whose neighbour counts are 60 % U{40..80} and 40 %
@@ -226,6 +228,140 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+LEARNED = dict(name="learned radial K=8 on the 4-species ord4 deg10 L10 model, 250k held-out envs, "
+                    "J 60% U{40..80} / 40% U{8..20}",
+               K=8, Q=8, student_deg=10, train_envs=50_000, neighbour_samples=2_000_000, eval_envs=250_000,
+               pretrain_steps=1500, distill_steps=2000, force_envs=300, force_weight=0.05, seed=2024)
+
+
+def mlp_flops_per_neighbour(mlp):
+    """Forward with the r-tangent: two matrix-vector products per layer."""
+    return 2 * 2 * (64 * mlp.D + 64 * 64 + mlp.C * 64)
+
+
+def run_learned(args, torch, dist, rank, world, local):
+    """The learned radial form on the 4-species workload: distil a K = 8
+    student from the plain model (FP64 labels), then time the student's
+    energies + forces on held-out environments and judge its error against
+    the plain FP64 evaluation."""
+    from ace_gb300 import learned as LR
+    from ace_gb300.configs import random_batch
+    from ace_gb300.lib import Context
+    from ace_gb300.spec import random_coefficients, symmetric_basis
+    W, X = WORKLOADS["ord4_deg10_4sp"], LEARNED
+    dev = torch.device("cuda", local)
+    t_setup = time.perf_counter()
+    teacher_spec = symmetric_basis(W["maxorder"], W["maxdeg"], maxL=W["maxL"], nspecies=W["nspecies"])
+    ct = random_coefficients(teacher_spec, seed=W["seed"])
+    teacher = Context(teacher_spec, "fp64", device=local)
+    teacher.set_params(ct)
+    train = random_batch(X["train_envs"], W["jlo"], W["jhi"], nspecies=W["nspecies"], seed=X["seed"] + 1,
+                         bimodal=W["bimodal"])
+    nenv = args.nenv or X["eval_envs"]
+    ev = random_batch(nenv, W["jlo"], W["jhi"], nspecies=W["nspecies"], seed=X["seed"] + 2, bimodal=W["bimodal"])
+    Etr, Gtr = teacher.energy_forces(train.offsets, train.rr, train.species)
+    sdeg = args.student_deg or X["student_deg"]
+    spec = LR.student_spec(W["maxorder"], sdeg, X["K"], W["maxL"])
+    nf = X["force_envs"]
+    fw = X["force_weight"] if args.force_weight is None else args.force_weight
+    forces = (LR.sub_batch(train, 0, nf), Gtr[:train.offsets[nf]], fw) if fw > 0 else None
+    mlp = LR.RadialMLP.init(spec, K=X["K"], nspecies=W["nspecies"], Q=X["Q"], seed=X["seed"])
+    ctx = LR.learned_context(spec, mlp, device=local)
+    t0 = time.perf_counter()
+    LR.pretrain_radial(ctx, mlp, spec, nsamples=X["neighbour_samples"], steps=X["pretrain_steps"])
+    c0 = LR.fit_coefficients(ctx, spec, LR.sub_batch(train, 0, 20000), Etr[:20000], forces=forces)
+    ctx.set_params(c0)
+    t1 = time.perf_counter()
+    # judge on the held-out set: FP64 plain evaluation (device path, chunked)
+    off_d = torch.from_numpy(ev.offsets).to(dev)
+    rr_d = torch.from_numpy(ev.rr).to(dev)
+    sp_d = torch.from_numpy(ev.species).to(dev)
+    E_d = torch.empty(nenv, dtype=torch.float64, device=dev)
+    G_d = torch.empty_like(rr_d)
+    teacher.energy_forces_device(off_d, rr_d, sp_d, E_d, G_d)
+    Eref, Gref = E_d.cpu().numpy().copy(), G_d.cpu().numpy().copy()
+
+    def judged():
+        ctx.energy_forces_device(off_d, rr_d, sp_d, E_d, G_d)
+        E, G = E_d.cpu().numpy(), G_d.cpu().numpy()
+        e = LR.energy_error(E, Eref)
+        e["F_rel_rmse"] = float(np.sqrt(np.mean((G - Gref) ** 2)) / np.sqrt(np.mean(Gref ** 2)))
+        return e
+    err_untrained = judged()
+    c1, hist = LR.distill(ctx, mlp, spec, train, Etr, c0, steps=X["distill_steps"], batch_envs=512, lr=1e-3,
+                          refit_every=500, refit_envs=20000, forces=forces)
+    t2 = time.perf_counter()
+    err = judged()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(args.warmup):
+        ctx.energy_forces_device(off_d, rr_d, sp_d, E_d, G_d, stream=stream.cuda_stream, sync=False)
+    torch.cuda.synchronize()
+    l0 = ctx.launch_count()
+    tot = 0.0
+    with Clocks(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            ctx.energy_forces_device(off_d, rr_d, sp_d, E_d, G_d, stream=stream.cuda_stream, sync=False)
+            e.record(stream)
+            e.synchronize()
+            tot += s.elapsed_time(e) / 1e3
+    launches = ctx.launch_count() - l0
+    value = nenv * args.steps / tot
+    # the plain forms on the same held-out batch (the teacher's basis)
+    t64 = 0.0
+    n64 = min(nenv, 20000)
+    teacher.energy_forces_device(off_d[:n64 + 1], rr_d, sp_d, E_d[:n64], G_d)
+    torch.cuda.synchronize()
+    for _ in range(2):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        teacher.energy_forces_device(off_d[:n64 + 1], rr_d, sp_d, E_d[:n64], G_d, stream=stream.cuda_stream,
+                                     sync=False)
+        e.record(stream)
+        e.synchronize()
+        t64 += s.elapsed_time(e) / 1e3
+    px2 = Context(teacher_spec, "fp32x2", device=local)
+    px2.set_params(ct)
+    px2.energy_forces_device(off_d, rr_d, sp_d, E_d, G_d)
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record(stream)
+    px2.energy_forces_device(off_d, rr_d, sp_d, E_d, G_d, stream=stream.cuda_stream, sync=False)
+    e.record(stream)
+    e.synchronize()
+    tx2 = s.elapsed_time(e) / 1e3
+    peaks = measured_peaks(torch)
+    Jmean = ev.nnbr / nenv
+    fl = (flops_per_env(spec, Jmean) + Jmean * mlp_flops_per_neighbour(mlp)) * nenv
+    achieved = fl / (tot / args.steps) / 1e12
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": X["name"], "nenv_per_gpu": nenv, "nnbr_per_gpu": int(ev.nnbr),
+                       "form": "learned radial (MLP 8 Chebyshev + 4 species -> 64 -> 64 -> 8 x 11 channels, "
+                               "FP32) + FP32 Ylm/A/AA/adjoint/forces on the student spec",
+                       "student": {"maxdeg": sdeg, "K": X["K"], "nA": spec.nA, "nAA": spec.nAA, "nB": spec.nB},
+                       "teacher": {"nA": teacher_spec.nA, "nAA": teacher_spec.nAA, "nB": teacher_spec.nB},
+                       "l2": "flushed (256 MB write) between timed steps"},
+            "error_vs_plain_fp64": err, "error_untrained_student": err_untrained,
+            "training": {"neighbour_samples": X["neighbour_samples"], "pretrain_steps": X["pretrain_steps"],
+                         "train_envs": X["train_envs"], "distill_steps": X["distill_steps"],
+                         "force_envs": nf if fw > 0 else 0, "force_weight": fw,
+                         "pretrain_s": t1 - t0, "distill_s": t2 - t1, "setup_s": t0 - t_setup,
+                         "loss_first_last": [hist[0], hist[-1]]},
+            "forms": {"learned_fp32": {"value": value},
+                      "plain_fp64": {"value": 2 * n64 / t64, "envs": n64},
+                      "plain_fp32x2": {"value": nenv / tx2}},
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peaks["fp32_tflops"], "unit": "TFLOP/s",
+                         "frac": achieved / peaks["fp32_tflops"], "traffic": None,
+                         "kernel": "mlp_fwd_kernel + ef_kernel<float> (learned radial form)",
+                         "flops_per_env": fl / nenv},
+            "clocks": clk.summary(), "gpu_launches": int(launches), "peaks_measured": peaks}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -235,10 +371,12 @@ def main():
     ap.add_argument("--nenv", type=int, default=None, help="smaller workload (profiling only)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", default="ord4_deg12", choices=sorted(WORKLOADS))
+    ap.add_argument("--student-deg", type=int, default=None, help="learned form: student spec degree")
+    ap.add_argument("--force-weight", type=float, default=None, help="learned form: weight of gradient rows")
+    ap.add_argument("--workload", default="ord4_deg12", choices=sorted(WORKLOADS) + ["learned_4sp"])
     args = ap.parse_args()
     global WORKLOAD
-    WORKLOAD = WORKLOADS[args.workload]
+    WORKLOAD = WORKLOADS.get(args.workload, WORKLOADS["ord4_deg12"])
     if args.impl == "reference":
         return run_reference(args)
 
@@ -255,6 +393,12 @@ def main():
         dist.barrier()
     from ace_gb300.lib import Context
 
+    if args.workload == "learned_4sp":
+        if rank == 0:
+            run_learned(args, torch, dist, rank, world, local)
+        if world > 1:
+            dist.barrier()
+        return
     spec, c, b = build_workload(args.nenv)
     nenv, nnbr = b.nenv, b.nnbr
     dev = torch.device("cuda", local)

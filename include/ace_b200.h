@@ -187,10 +187,12 @@ int ace_autotune(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, const doubl
    C = K (L + 1), row-major FP32.  The context's spec must be single-species
    with nR = K; A entry (n, l, m) then reads channel (n - 1) + K l.  After
    ace_set_radial_mlp the context's ace_energy_forces / ace_energy /
-   ace_basis evaluate the learned form (species index the MLP's one-hot);
-   ace_basis with dB, ace_adjoint_eval_d and ace_basis_noalloc return
-   ACE_ERR_UNSUPPORTED.  The training entry points below take device
-   pointers only and run asynchronously on `stream`. */
+   ace_basis / ace_adjoint_eval_d evaluate the learned form (species index
+   the MLP's one-hot); ace_basis_noalloc returns ACE_ERR_UNSUPPORTED.  Each
+   learned-form call reads the batch's neighbour count back to the host (to
+   size its radial buffer) and so synchronises its stream.  The training
+   entry points below take device pointers only and run asynchronously on
+   `stream`. */
 typedef struct ace_radial_mlp {
   int32_t version;  /* 1 */
   int32_t K, Q, nspecies, H;

@@ -172,3 +172,19 @@ def test_distillation_gain_and_fallback(lib):
     assert np.allclose(G[o0:o1], Gt2[o0:o1], rtol=1e-10, atol=1e-14)
     Es, _ = model.ctx.energy_forces(test.offsets, rr, test.species)
     assert np.allclose(E[ok], Es[ok], rtol=1e-12, atol=0)
+
+
+def test_learned_basis_and_derivative(lib, oracle_mod, student):
+    """B and dB of the learned form (FP32) against the oracle fed the same
+    radial channels: 1e-5 (B) and 1e-4 (dB) relative to the largest
+    magnitude."""
+    spec, mlp = student
+    ctx = learned_context(spec, mlp)
+    b = random_batch(20, 5, 15, nspecies=NS, seed=12)
+    B, dB = ctx.basis(b.offsets, b.rr, b.species, grad=True)
+    orc = oracle_mod.Oracle(spec, np.zeros(spec.nB), channels_per_l=K)
+    R, dR = _oracle_inputs(spec, mlp, b)
+    orc.set_radial(R, dR)
+    Bref, dBref = orc.basis_d(b.offsets, b.rr, b.species)
+    assert relerr(B, Bref) <= 1e-5
+    assert relerr(dB, dBref) <= 1e-4
