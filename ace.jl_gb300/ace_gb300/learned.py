@@ -211,10 +211,10 @@ def fit_coefficients(ctx: Context, spec: ACESpec, b: Batch, E_target: np.ndarray
         G += w * (D.T @ D) / (len(g) * sf)
         rhs += w * (D.T @ g) / (len(g) * sf)
         del D
-    lam = ridge * float(torch.trace(G)) / nB
-    G += lam * torch.eye(nB, dtype=G.dtype, device=dev)
-    c = torch.linalg.solve(G, rhs)
-    return c.cpu().numpy()
+    # the normal equations are nB x nB: solved on the host
+    Gh, rh = G.cpu().numpy(), rhs.cpu().numpy()
+    Gh[np.diag_indices(nB)] += ridge * np.trace(Gh) / nB
+    return np.linalg.solve(Gh, rh)
 
 
 def sub_batch(b: Batch, e0: int, e1: int) -> Batch:

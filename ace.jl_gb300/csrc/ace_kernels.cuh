@@ -36,6 +36,11 @@ namespace ace {
 
 __host__ __device__ inline size_t al16(size_t x) { return (x + 15) & ~size_t(15); }
 
+// items per thread and iteration in the item-schedule correlation phase
+#ifndef EF_ITEM_ILP
+#define EF_ITEM_ILP 2
+#endif
+
 struct EFArgs {
   int64_t nEnv;
   const int64_t *off;
@@ -315,65 +320,96 @@ __global__ void __launch_bounds__(NT) ef_kernel(EFArgs a) {
       if (d <= cur) close(d);
       eacc = H[0].re;
     } else {
+      // EF_ITEM_ILP items per thread and iteration, interleaved: their
+      // product chains and warp reductions are independent, which hides the
+      // latency of the dependent double-float arithmetic
       constexpr int KP = (K > 1) ? K - 1 : 1;
+      constexpr int IU = EF_ITEM_ILP;
       const int lane = tid & 31;
       const cpx<TG> gone = {TG(1), TG(0)};
-      for (int64_t f = tid; f < a.in; f += NT) {
-        const uint4 rc = a.irec[f];
-        const int P = (rc.w >> 16) & 0xf, nl = (rc.w >> 20) & 0xf;
-        const unsigned heads = (rc.w >> 24) & 0xff;
-        const uint32_t vw[4] = {rc.x, rc.y, rc.z, rc.w};
-        cpx<TE> bar = {Arith<TE>::one(), Arith<TE>::zero()};
-        cpx<TG> aG[KP];
-        int vi[KP];
+      const TE ze = Arith<TE>::zero();
+      for (int64_t f0 = tid; f0 < a.in; f0 += (int64_t)IU * NT) {
+        int P[IU], nl[IU], vi[IU][KP], ul[IU][ITEM_G];
+        unsigned heads[IU];
+        cpx<TE> bar[IU], H[IU];
+        cpx<TG> aG[IU][KP];
+        TE cl[IU][ITEM_G];
 #pragma unroll
-        for (int d = 0; d < KP; ++d) {
-          vi[d] = (int)((vw[d >> 1] >> (16 * (d & 1))) & 0xffff);
-          aG[d] = gone;
-          if (d < P) {
-            const cpx<TE> ae = AE[vi[d]];
-            bar = (d == 0) ? ae : cmul(bar, ae);
-            if (GRAD) aG[d] = AG[vi[d]];
-          }
-        }
-        cpx<TE> H = {load_coef<TE>(a.ic, f), Arith<TE>::zero()};
-        TE cl[ITEM_G];
-        int ul[ITEM_G];
-#pragma unroll
-        for (int g = 0; g < ITEM_G; ++g) {
-          ul[g] = (int)((vw[(5 + g) >> 1] >> (16 * ((5 + g) & 1))) & 0xffff);
-          cl[g] = load_coef<TE>(a.ic, (int64_t)(g + 1) * a.in + f);
-          if (g < nl) H = cadd(H, cscale(AE[ul[g]], cl[g]));
-        }
-        if (P > 0) eacc = eacc + (bar.re * H.re - bar.im * H.im);
-        if (GRAD) {
-          cpx<TG> pre[KP], suf[KP];
-          pre[0] = gone;
-#pragma unroll
-          for (int d = 1; d < KP; ++d) pre[d] = (d < P) ? cmul(pre[d - 1], aG[d - 1]) : pre[d - 1];
-          suf[KP - 1] = gone;
-#pragma unroll
-          for (int d = KP - 2; d >= 0; --d) suf[d] = (d + 1 < P) ? cmul(aG[d + 1], suf[d + 1]) : gone;
-          const cpx<TG> bG = cmul(pre[KP - 1], aG[KP - 1]);
-          const cpx<TG> h = {lower<TG>(H.re), lower<TG>(H.im)};
-#pragma unroll
-          for (int g = 0; g < ITEM_G; ++g)
-            if (g < nl) dacc(ul[g], cscale(bG, lower<TG>(cl[g])));
+        for (int u = 0; u < IU; ++u) {
+          const int64_t f = f0 + (int64_t)u * NT;
+          // item_n is a multiple of NT, so `ok` is uniform across the CTA
+          const bool ok = f < a.in;
+          const uint4 rc = ok ? a.irec[f] : make_uint4(0u, 0u, 0u, 0u);
+          P[u] = (rc.w >> 16) & 0xf;
+          nl[u] = (rc.w >> 20) & 0xf;
+          heads[u] = (rc.w >> 24) & 0xff;
+          const uint32_t vw[4] = {rc.x, rc.y, rc.z, rc.w};
+          bar[u] = {Arith<TE>::one(), ze};
 #pragma unroll
           for (int d = 0; d < KP; ++d) {
-            cpx<TG> v = (d < P) ? cmul(cmul(pre[d], suf[d]), h) : cpx<TG>{TG(0), TG(0)};
+            vi[u][d] = (int)((vw[d >> 1] >> (16 * (d & 1))) & 0xffff);
+            aG[u][d] = gone;
+            if (d < P[u]) {
+              const cpx<TE> ae = AE[vi[u][d]];
+              bar[u] = (d == 0) ? ae : cmul(bar[u], ae);
+              if (GRAD) aG[u][d] = AG[vi[u][d]];
+            }
+          }
+          H[u] = {ok ? load_coef<TE>(a.ic, f) : ze, ze};
+#pragma unroll
+          for (int g = 0; g < ITEM_G; ++g) {
+            ul[u][g] = (int)((vw[(5 + g) >> 1] >> (16 * ((5 + g) & 1))) & 0xffff);
+            cl[u][g] = ok ? load_coef<TE>(a.ic, (int64_t)(g + 1) * a.in + f) : ze;
+            if (g < nl[u]) H[u] = cadd(H[u], cscale(AE[ul[u][g]], cl[u][g]));
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < IU; ++u)
+          if (P[u] > 0) eacc = eacc + (bar[u].re * H[u].re - bar[u].im * H[u].im);
+        if (GRAD) {
+          cpx<TG> v[IU][KP];
+#pragma unroll
+          for (int u = 0; u < IU; ++u) {
+            cpx<TG> pre[KP], suf[KP];
+            pre[0] = gone;
+#pragma unroll
+            for (int d = 1; d < KP; ++d) pre[d] = (d < P[u]) ? cmul(pre[d - 1], aG[u][d - 1]) : pre[d - 1];
+            suf[KP - 1] = gone;
+#pragma unroll
+            for (int d = KP - 2; d >= 0; --d) suf[d] = (d + 1 < P[u]) ? cmul(aG[u][d + 1], suf[d + 1]) : gone;
+            const cpx<TG> bG = cmul(pre[KP - 1], aG[u][KP - 1]);
+            const cpx<TG> h = {lower<TG>(H[u].re), lower<TG>(H[u].im)};
+#pragma unroll
+            for (int g = 0; g < ITEM_G; ++g)
+              if (g < nl[u]) dacc(ul[u][g], cscale(bG, lower<TG>(cl[u][g])));
+#pragma unroll
+            for (int d = 0; d < KP; ++d)
+              v[u][d] = (d < P[u]) ? cmul(cmul(pre[d], suf[d]), h) : cpx<TG>{TG(0), TG(0)};
+          }
+#pragma unroll
+          for (int d = 0; d < KP; ++d) {
             if (d < KP - 1) {
               // runs of equal (v1..v_{d+1}) are adjacent lanes: reduce into each run's head
-              const unsigned hm = __ballot_sync(0xffffffffu, (heads >> d) & 1u);
+              unsigned hm[IU];
+#pragma unroll
+              for (int u = 0; u < IU; ++u) hm[u] = __ballot_sync(0xffffffffu, (heads[u] >> d) & 1u);
 #pragma unroll
               for (int off = 1; off < 32; off <<= 1) {
-                const cpx<TG> o = shfl_down_c(v, off);
-                const unsigned between = (unsigned)(((unsigned long long)hm >> (lane + 1)) & ((1ull << off) - 1ull));
-                if (lane + off < 32 && between == 0u) { v.re += o.re; v.im += o.im; }
+#pragma unroll
+                for (int u = 0; u < IU; ++u) {
+                  const cpx<TG> o = shfl_down_c(v[u][d], off);
+                  const unsigned between =
+                      (unsigned)(((unsigned long long)hm[u] >> (lane + 1)) & ((1ull << off) - 1ull));
+                  if (lane + off < 32 && between == 0u) { v[u][d].re += o.re; v[u][d].im += o.im; }
+                }
               }
-              if (((heads >> d) & 1u) && d < P) dacc(vi[d], v);
-            } else if (d < P) {
-              dacc(vi[d], v);
+#pragma unroll
+              for (int u = 0; u < IU; ++u)
+                if (((heads[u] >> d) & 1u) && d < P[u]) dacc(vi[u][d], v[u][d]);
+            } else {
+#pragma unroll
+              for (int u = 0; u < IU; ++u)
+                if (d < P[u]) dacc(vi[u][d], v[u][d]);
             }
           }
         }

@@ -268,7 +268,9 @@ def run_learned(args, torch, dist, rank, world, local):
     mlp = LR.RadialMLP.init(spec, K=X["K"], nspecies=W["nspecies"], Q=X["Q"], seed=X["seed"])
     ctx = LR.learned_context(spec, mlp, device=local)
     t0 = time.perf_counter()
-    LR.pretrain_radial(ctx, mlp, spec, nsamples=X["neighbour_samples"], steps=X["pretrain_steps"])
+    psteps = X["pretrain_steps"] if args.pretrain_steps is None else args.pretrain_steps
+    dsteps = X["distill_steps"] if args.distill_steps is None else args.distill_steps
+    LR.pretrain_radial(ctx, mlp, spec, nsamples=X["neighbour_samples"], steps=psteps)
     c0 = LR.fit_coefficients(ctx, spec, LR.sub_batch(train, 0, 20000), Etr[:20000], forces=forces)
     ctx.set_params(c0)
     t1 = time.perf_counter()
@@ -288,7 +290,7 @@ def run_learned(args, torch, dist, rank, world, local):
         e["F_rel_rmse"] = float(np.sqrt(np.mean((G - Gref) ** 2)) / np.sqrt(np.mean(Gref ** 2)))
         return e
     err_untrained = judged()
-    c1, hist = LR.distill(ctx, mlp, spec, train, Etr, c0, steps=X["distill_steps"], batch_envs=512, lr=1e-3,
+    c1, hist = LR.distill(ctx, mlp, spec, train, Etr, c0, steps=dsteps, batch_envs=512, lr=1e-3,
                           refit_every=500, refit_envs=20000, forces=forces)
     t2 = time.perf_counter()
     err = judged()
@@ -346,11 +348,11 @@ def run_learned(args, torch, dist, rank, world, local):
                        "teacher": {"nA": teacher_spec.nA, "nAA": teacher_spec.nAA, "nB": teacher_spec.nB},
                        "l2": "flushed (256 MB write) between timed steps"},
             "error_vs_plain_fp64": err, "error_untrained_student": err_untrained,
-            "training": {"neighbour_samples": X["neighbour_samples"], "pretrain_steps": X["pretrain_steps"],
-                         "train_envs": X["train_envs"], "distill_steps": X["distill_steps"],
+            "training": {"neighbour_samples": X["neighbour_samples"], "pretrain_steps": psteps,
+                         "train_envs": X["train_envs"], "distill_steps": dsteps,
                          "force_envs": nf if fw > 0 else 0, "force_weight": fw,
                          "pretrain_s": t1 - t0, "distill_s": t2 - t1, "setup_s": t0 - t_setup,
-                         "loss_first_last": [hist[0], hist[-1]]},
+                         "loss_first_last": [hist[0], hist[-1]] if hist else None},
             "forms": {"learned_fp32": {"value": value},
                       "plain_fp64": {"value": 2 * n64 / t64, "envs": n64},
                       "plain_fp32x2": {"value": nenv / tx2}},
@@ -373,6 +375,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--student-deg", type=int, default=None, help="learned form: student spec degree")
     ap.add_argument("--force-weight", type=float, default=None, help="learned form: weight of gradient rows")
+    ap.add_argument("--pretrain-steps", type=int, default=None, help="learned form: radial pretraining steps")
+    ap.add_argument("--distill-steps", type=int, default=None, help="learned form: distillation steps")
     ap.add_argument("--workload", default="ord4_deg12", choices=sorted(WORKLOADS) + ["learned_4sp"])
     args = ap.parse_args()
     global WORKLOAD
