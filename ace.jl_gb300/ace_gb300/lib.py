@@ -211,6 +211,13 @@ class Context:
                                        _ptr(B), _ptr(dB), 0, None))
         return (B, dB) if grad else B
 
+    def basis_device(self, offsets, rr, species, B, stream=None, sync=True):
+        """B (nEnv, nB) of device inputs into a device tensor."""
+        flags = ACE_INPUTS_ON_DEVICE | ACE_OUTPUTS_ON_DEVICE | (0 if sync else ACE_ASYNC)
+        st = None if stream is None else C.c_void_p(int(stream))
+        self._check(self.lib.ace_basis(self.h, B.shape[0], _ptr(offsets), _ptr(rr), _ptr(species), _ptr(B), None,
+                                       flags, st))
+
     def basis_to_device(self, offsets, rr, species, B, dB=None):
         """B (and dB) of host inputs into device tensors B (nEnv, nB) and dB
         (nNbr, nB, 3)."""

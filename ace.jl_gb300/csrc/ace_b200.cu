@@ -41,6 +41,8 @@ template <typename T> static int upload(ace_ctx *ctx, T **dst, const T *src, siz
   return ACE_OK;
 }
 
+static int pack_coefs(ace_ctx *ctx, void *dst, int64_t n, const std::function<double(int64_t)> &val);
+
 // Coefficient table (layout documented in ace_phi.cuh).
 static std::vector<double> coef_table(const ace_spec_bundle *s, int L) {
   const int szP = size_p(L);
@@ -240,6 +242,32 @@ extern "C" int ace_ctx_create(const ace_spec_bundle *s, int32_t prec, int32_t de
         (rc = upload(ctx, &ctx->d_UvalF, uf.data(), uf.size()))) {
       g_create_error = ctx->err;
       return fail(rc);
+    }
+    // fused basis table for the FP32-based forms (measured faster there); the
+    // FP64 form keeps the AA-scratch path, whose flat products are fewer
+    // (nAA instead of nnz(U)).  ACE_B200_BASIS=fused|materialised overrides.
+    const char *benv = getenv("ACE_B200_BASIS");
+    ctx->fused_basis = (prec != ACE_PREC_FP64);
+    if (benv && std::string(benv) == "materialised") ctx->fused_basis = false;
+    if (benv && std::string(benv) == "fused") ctx->fused_basis = true;
+    if (s->nB >= (int64_t(1) << 27)) ctx->fused_basis = false;
+    if (ctx->fused_basis) {
+      URows ur = build_urows(s->nB, s->U_indptr, s->U_indices, s->U_data, s->orders, s->iAA2iA, s->maxord, 128);
+      ctx->ulen = ur.len;
+      const size_t csz = (prec == ACE_PREC_FP32 || prec == ACE_PREC_FP32_BF16X3) ? 4 : 8;
+      if ((rc = upload(ctx, (uint32_t **)&ctx->d_urec, ur.rec.data(), ur.rec.size()))) {
+        g_create_error = ctx->err;
+        return fail(rc);
+      }
+      if (cudaMalloc(&ctx->d_uval, std::max<size_t>(ur.val.size(), 1) * csz) != cudaSuccess) {
+        g_create_error = "cudaMalloc failed";
+        return fail(ACE_ERR_ALLOC);
+      }
+      ctx->allocs.push_back(ctx->d_uval);
+      if ((rc = pack_coefs(ctx, ctx->d_uval, (int64_t)ur.val.size(), [&](int64_t j) { return ur.val[j]; }))) {
+        g_create_error = ctx->err;
+        return fail(rc);
+      }
     }
   }
   // status word

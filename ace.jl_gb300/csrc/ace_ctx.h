@@ -79,6 +79,13 @@ struct ace_ctx {
   size_t smem = 0;
   int aa_chunk = 32, aa_grid = 0;
   size_t aa_smem = 0;
+  // fused symmetric basis (ace_sched.h build_urows); false: AA materialised
+  bool fused_basis = true;
+  int64_t ulen = 0;
+  uint4 *d_urec = nullptr;
+  void *d_uval = nullptr;      // U values in the energy type, slot order
+  int ub_chunk = 8, ub_grid = 0;
+  size_t ub_smem = 0;
 
   // learned radial form (ace_set_radial_mlp): the spec's radial index n is a
   // channel k < K of an MLP (transform features, species one-hot) -> K (L+1)

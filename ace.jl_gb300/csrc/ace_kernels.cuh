@@ -569,6 +569,63 @@ __global__ void ub_kernel(int64_t ne, int64_t e0, int64_t ldE, int64_t nB, const
   }
 }
 
+// Fused B = U real(AA) per environment, without AA in memory: phase 1 (A in
+// shared memory), then each thread walks its U rows' entries (ace_sched.h
+// build_urows), forms real(AA_k) = Re(prod A) (src/pibasis.jl:265-275) and
+// accumulates U[b, k] real(AA_k); a row's sum is written at its last entry
+// (genmul!, src/symmbasis.jl:248-264).
+template <typename TE>
+__global__ void __launch_bounds__(128) ub_fused_kernel(EFArgs a, const uint4 *urec, const void *uval, int64_t ulen,
+                                                       int64_t nB, double *B) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  const EFLayout lay = ef_layout(a.ntab, a.nRs, a.L, a.nA, a.chunkE, 1, 0, 128, sizeof(TE), sizeof(TE), true);
+  TE *tabE = (TE *)(sm + lay.tabE);
+  int16_t *s_an = (int16_t *)(sm + lay.an);
+  int16_t *s_aiy = (int16_t *)(sm + lay.aiy);
+  int16_t *s_amu = (int16_t *)(sm + lay.amu);
+  cpx<TE> *AE = (cpx<TE> *)(sm + lay.AE);
+  int *ssp = (int *)(sm + lay.spc);
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int i = tid; i < a.ntab; i += nt) tabE[i] = load_table<TE>(a.tabE, i);
+  for (int i = tid; i < a.nA; i += nt) { s_an[i] = a.an[i]; s_aiy[i] = a.aiy[i]; s_amu[i] = a.amu[i]; }
+  __syncthreads();
+  Tables<TE> tb;
+  tb.bind(tabE, a.nR, a.L, a.pl, a.pr, a.tp);
+  const int64_t ntot = a.off[a.nEnv];
+  const TE ze = Arith<TE>::zero();
+  for (int64_t e = blockIdx.x; e < a.nEnv; e += gridDim.x) {
+    const int64_t o0 = a.off[e], o1 = a.off[e + 1];
+    if (o0 < 0 || o1 < o0 || o1 > ntot) {
+      if (tid == 0) atomicOr(a.status, ACE_STATUS_BAD_OFFSETS);
+      continue;
+    }
+    build_A<TE>(a, tb, o0, (int)(o1 - o0), a.chunkE, lay.slabE, s_an, s_aiy, s_amu, ssp, (TE *)(sm + lay.slab), AE);
+    TE acc = ze;
+    double *Be = B + e * nB;
+    for (int64_t j = 0; j < ulen; ++j) {
+      const int64_t slot = j * nt + tid;
+      const uint4 rc = urec[slot];
+      if (!(rc.w >> 31)) break;  // padding only follows a thread's last entry
+      const int ord = (rc.w >> 27) & 7;
+      const uint32_t vw[3] = {rc.x, rc.y, rc.z};
+      cpx<TE> p = {Arith<TE>::one(), ze};
+#pragma unroll
+      for (int t = 0; t < 6; ++t) {
+        if (t < ord) {
+          const cpx<TE> av = AE[(vw[t >> 1] >> (16 * (t & 1))) & 0xffff];
+          p = (t == 0) ? av : cmul(p, av);
+        }
+      }
+      acc = acc + load_coef<TE>(uval, slot) * p.re;
+      if ((rc.w >> 30) & 1u) {
+        Be[rc.w & ((1u << 27) - 1u)] = lower<double>(acc);
+        acc = ze;
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // Kernel arguments for a context (host side).
 inline EFArgs make_args(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const double *rr, const int32_t *sp,
                         double *E, double *G) {

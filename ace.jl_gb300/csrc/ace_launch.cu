@@ -45,6 +45,14 @@ static void *aa_func(const ace_ctx *ctx) {
   }
 }
 
+static void *ub_func(const ace_ctx *ctx) {
+  switch (ctx->prec) {
+    case ACE_PREC_FP64: return (void *)ub_fused_kernel<double>;
+    case ACE_PREC_FP32X2: return (void *)ub_fused_kernel<df>;
+    default: return (void *)ub_fused_kernel<float>;
+  }
+}
+
 static void type_sizes(const ace_ctx *ctx, int &sE, int &sG, bool &same) {
   switch (ctx->prec) {
     case ACE_PREC_FP64: sE = 8; sG = 8; same = true; break;
@@ -105,6 +113,18 @@ int kernels_prepare(ace_ctx *ctx) {
   int occa = 1;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occa, fa, 256, la.total);
   ctx->aa_grid = ctx->nsm * std::max(occa, 1);
+  // fused basis: 128 threads, neighbour slabs within 16 KB
+  ctx->ub_chunk = std::max(1, std::min(128 / (ctx->L + 1), (16 * 1024) / slabE));
+  EFLayout lu = ef_layout(ctx->ntab, nRs, ctx->L, ctx->nA, ctx->ub_chunk, 1, 0, 128, sE, sE, true);
+  ctx->ub_smem = lu.total;
+  void *fu = ub_func(ctx);
+  if (cudaFuncSetAttribute(fu, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lu.total) != cudaSuccess) {
+    ctx->err = "cudaFuncSetAttribute failed";
+    return ACE_ERR_CUDA;
+  }
+  int occu = 1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occu, fu, 128, lu.total);
+  ctx->ub_grid = ctx->nsm * std::max(occu, 1);
   return ACE_OK;
 }
 
@@ -157,6 +177,19 @@ int launch_basis(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const double *r
   if (ctx->learned) {
     int rc = learned_radials(ctx, nEnv, off, rr, sp, st);
     if (rc) return rc;
+  }
+  if (ctx->fused_basis) {
+    EFArgs a = make_args(ctx, nEnv, off, rr, sp, nullptr, nullptr);
+    a.chunkE = ctx->ub_chunk;
+    const uint4 *urec = ctx->d_urec;
+    const void *uval = ctx->d_uval;
+    int64_t ulen = ctx->ulen, nB = ctx->nB;
+    const int grid = (int)std::min<int64_t>(nEnv, ctx->ub_grid);
+    void *args[] = {&a, &urec, &uval, &ulen, &nB, &B};
+    cudaError_t e = cudaLaunchKernel(ub_func(ctx), dim3(grid), dim3(128), args, ctx->ub_smem, st);
+    ctx->launches += 1;
+    if (e != cudaSuccess) { ctx->err = cudaGetErrorString(e); return ACE_ERR_CUDA; }
+    return ACE_OK;
   }
   const bool f32 = (ctx->prec == ACE_PREC_FP32 || ctx->prec == ACE_PREC_FP32_BF16X3);
   const size_t ts = f32 ? 4 : 8;

@@ -21,6 +21,7 @@
 #include <cmath>
 #include <cstdint>
 #include <map>
+#include <queue>
 #include <numeric>
 #include <vector>
 
@@ -256,6 +257,66 @@ inline ItemSchedule build_items(const Schedule &s, int nthreads) {
   }
   for (int64_t f = n0; f < it.n; ++f) ((uint8_t *)&it.rec[8 * f])[15] = 0x1f;  // padding: own segments
   return it;
+}
+
+// Fused symmetric-basis table (B = U real(AA) without AA in memory): the
+// nonzeros of U in row order, rows assigned to threads longest first, each to
+// the least-loaded thread, and each thread's entries interleaved
+// (slot = j * nthreads + thread) so a warp's loads are contiguous.  Record
+// (16 bytes): x, y, z = the AA function's A indices v0..v5 (uint16 pairs),
+// w = row | ord << 27 | last-of-row << 30 | valid << 31.  A row without
+// nonzeros gets one entry of value 0 so that its B value is written.
+struct URows {
+  int64_t len = 0;                 // slots per thread
+  std::vector<uint32_t> rec;       // [len * nthreads * 4]
+  std::vector<double> val;         // [len * nthreads]
+};
+
+inline URows build_urows(int64_t nB, const int64_t *Uptr, const int32_t *Uidx, const double *Uval,
+                         const int32_t *orders, const int32_t *iAA2iA, int K, int nthreads) {
+  URows u;
+  std::vector<int64_t> rows(nB);
+  for (int64_t b = 0; b < nB; ++b) rows[b] = b;
+  auto rlen = [&](int64_t b) { return std::max<int64_t>(1, Uptr[b + 1] - Uptr[b]); };
+  std::stable_sort(rows.begin(), rows.end(), [&](int64_t x, int64_t y) { return rlen(x) > rlen(y); });
+  std::vector<std::vector<int64_t>> own(nthreads);
+  std::vector<int64_t> load(nthreads, 0);
+  using P = std::pair<int64_t, int>;
+  std::priority_queue<P, std::vector<P>, std::greater<P>> pq;
+  for (int t = 0; t < nthreads; ++t) pq.push({0, t});
+  for (int64_t b : rows) {
+    P top = pq.top();
+    pq.pop();
+    own[top.second].push_back(b);
+    top.first += rlen(b);
+    load[top.second] = top.first;
+    pq.push(top);
+  }
+  for (int t = 0; t < nthreads; ++t) u.len = std::max(u.len, load[t]);
+  u.rec.assign((size_t)u.len * nthreads * 4, 0u);
+  u.val.assign((size_t)u.len * nthreads, 0.0);
+  for (int t = 0; t < nthreads; ++t) {
+    int64_t j = 0;
+    for (int64_t b : own[t]) {
+      const int64_t k0 = Uptr[b], k1 = Uptr[b + 1];
+      for (int64_t q = k0; q < std::max(k1, k0 + 1); ++q, ++j) {
+        const size_t slot = (size_t)j * nthreads + t;
+        uint32_t *r = &u.rec[4 * slot];
+        const bool empty = (k1 == k0);
+        const int64_t k = empty ? -1 : Uidx[q];
+        const int ord = empty ? 0 : orders[k];
+        uint16_t v[6] = {0, 0, 0, 0, 0, 0};
+        for (int d = 0; d < ord; ++d) v[d] = (uint16_t)iAA2iA[k * K + d];
+        r[0] = v[0] | ((uint32_t)v[1] << 16);
+        r[1] = v[2] | ((uint32_t)v[3] << 16);
+        r[2] = v[4] | ((uint32_t)v[5] << 16);
+        const bool last = (q + 1 >= std::max(k1, k0 + 1));
+        r[3] = (uint32_t)b | ((uint32_t)ord << 27) | ((last ? 1u : 0u) << 30) | (1u << 31);
+        u.val[slot] = empty ? 0.0 : Uval[q];
+      }
+    }
+  }
+  return u;
 }
 
 }  // namespace ace

@@ -473,6 +473,37 @@ def main():
     value = nenv * args.steps * world / t32
     ms = 1e3 * t32 / args.steps
 
+    # the symmetric basis B = U real(AA) (grad_params, the design matrix), FP64
+    # and fp32x2, on a prefix of the batch with B within 4 GB
+    nbe = int(min(nenv, max(1, (4 << 30) // (8 * spec.nB))))
+    B_d = torch.empty((nbe, spec.nB), dtype=torch.float64, device=dev)
+    basis = {}
+    Bref = None
+    for name, cx in (("basis_fp64", ctx64), ("basis_fp32x2", ctx)):
+        for _ in range(max(1, args.warmup)):
+            cx.basis_device(off_d[:nbe + 1], rr_d, sp_d, B_d, stream=stream.cuda_stream, sync=False)
+        torch.cuda.synchronize()
+        tb = 0.0
+        kb = max(1, min(args.steps, 5))
+        for _ in range(kb):
+            flush.zero_()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            cx.basis_device(off_d[:nbe + 1], rr_d, sp_d, B_d, stream=stream.cuda_stream, sync=False)
+            e.record(stream)
+            e.synchronize()
+            tb += s.elapsed_time(e) / 1e3
+        cx.sync()
+        basis[name] = {"value": nbe * kb / tb, "ms_per_step": 1e3 * tb / kb, "envs": nbe,
+                       "B_bytes_per_env": 8 * spec.nB}
+        if Bref is None:
+            Bref = B_d.cpu().numpy().copy()
+        else:
+            Bx = B_d.cpu().numpy()
+            basis[name]["error"] = {"B_rel_max_vs_fp64": float(np.max(np.abs(Bx - Bref)) / np.max(np.abs(Bref)))}
+    del B_d, Bref
+    torch.cuda.empty_cache()
+
     # e2e through the C ABI with pinned host buffers
     e2e = None
     if not args.no_e2e:
@@ -534,7 +565,7 @@ def main():
             "forms": {"fp64": {"value": n64 * k64 * world / t64, "ms_per_step": 1e3 * t64 / k64, "envs": n64},
                       "fp32": {"value": nenv * args.steps * world / t32p, "ms_per_step": 1e3 * t32p / args.steps,
                                "error": err32},
-                      "fp32x2": {"value": value, "ms_per_step": ms, "error": err}},
+                      "fp32x2": {"value": value, "ms_per_step": ms, "error": err}, **basis},
             "error": err, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
             "gpu_launches": int(launches), "peaks_measured": peaks}
     print(json.dumps(line), flush=True)

@@ -90,13 +90,18 @@ def test_multispecies(lib, oracle_mod, prec):
 
 
 @pytest.mark.parametrize("prec", ["fp64", "fp32", "fp32x2"])
-def test_basis(lib, oracle_mod, prec):
-    spec = get_spec("cfg1")
-    b = random_batch(300, 12, 24, seed=4)
+@pytest.mark.parametrize("path", ["fused", "materialised"])
+@pytest.mark.parametrize("name,nenv,ns", [("cfg1", 300, 1), ("cfg2", 40, 1), ("species", 30, 3)])
+def test_basis(lib, oracle_mod, prec, path, name, nenv, ns, monkeypatch):
+    """B = U real(AA): the fused kernel (AA never in memory) and the
+    AA-scratch path, against the oracle."""
+    monkeypatch.setenv("ACE_B200_BASIS", path)
+    spec = symmetric_basis(3, 6, maxL=6, nspecies=3) if name == "species" else get_spec(name)
+    b = random_batch(nenv, 12, 24, nspecies=ns, seed=4)
     orc = oracle_mod.Oracle(spec)
-    Bref = orc.basis(b.offsets, b.rr)
+    Bref = orc.basis(b.offsets, b.rr, b.species)
     ctx = lib.Context(spec, prec)
-    B = ctx.basis(b.offsets, b.rr)
+    B = ctx.basis(b.offsets, b.rr, b.species)
     assert relerr(B, Bref) <= TOL[prec]["B"]
 
 
