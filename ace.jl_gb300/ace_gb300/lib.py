@@ -26,7 +26,7 @@ EXPORTED = ("ace_ctx_create", "ace_ctx_destroy", "ace_set_params", "ace_set_ctil
             "ace_last_error_string", "ace_launch_count", "ace_basis_noalloc", "ace_adjoint_eval_d",
             "ace_set_params_multi", "ace_energy_forces_multi", "ace_autotune", "ace_set_radial_mlp",
             "ace_radial_mlp_params", "ace_radial_mlp_forward", "ace_radial_mlp_backward",
-            "ace_energy_radial_adjoint", "ace_adam_step", "ace_radial_mlp_get_params")
+            "ace_energy_radial_adjoint", "ace_adam_step", "ace_radial_mlp_get_params", "ace_radial_mlp_infer")
 
 
 class AceError(RuntimeError):
@@ -83,6 +83,7 @@ def load(path: str | None = None):
     lib.ace_radial_mlp_params.argtypes = [P, P, P]
     lib.ace_radial_mlp_forward.argtypes = [P, C.c_int64, P, P, P, P]
     lib.ace_radial_mlp_get_params.argtypes = [P, P, C.c_int32]
+    lib.ace_radial_mlp_infer.argtypes = [P, C.c_int64, P, P, P, P]
     lib.ace_radial_mlp_backward.argtypes = [P, C.c_int64, P, P, P, P, P, P]
     lib.ace_energy_radial_adjoint.argtypes = [P, C.c_int64, P, P, P, P, P, P, P]
     lib.ace_adam_step.argtypes = [C.c_int64, P, P, P, P, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int32, P]
@@ -97,7 +98,8 @@ def load(path: str | None = None):
                  "ace_basis_noalloc", "ace_adjoint_eval_d",
             "ace_set_params_multi", "ace_energy_forces_multi", "ace_autotune", "ace_set_radial_mlp",
                  "ace_radial_mlp_params", "ace_radial_mlp_forward", "ace_radial_mlp_backward",
-                 "ace_energy_radial_adjoint", "ace_adam_step", "ace_radial_mlp_get_params"):
+                 "ace_energy_radial_adjoint", "ace_adam_step", "ace_radial_mlp_get_params",
+                 "ace_radial_mlp_infer"):
         getattr(lib, name).restype = C.c_int
     _lib = lib
     return lib
@@ -295,6 +297,10 @@ class Context:
     def radial_mlp_forward(self, rr, species, R, stream=None):
         st = None if stream is None else C.c_void_p(int(stream))
         self._check(self.lib.ace_radial_mlp_forward(self.h, rr.shape[0], _ptr(rr), _ptr(species), _ptr(R), st))
+
+    def radial_mlp_infer(self, rr, species, R, stream=None):
+        st = None if stream is None else C.c_void_p(int(stream))
+        self._check(self.lib.ace_radial_mlp_infer(self.h, rr.shape[0], _ptr(rr), _ptr(species), _ptr(R), st))
 
     def radial_mlp_backward(self, rr, species, gR, wj, gparams, stream=None):
         st = None if stream is None else C.c_void_p(int(stream))

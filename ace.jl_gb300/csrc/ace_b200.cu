@@ -457,6 +457,7 @@ static int read_status(ace_ctx *ctx, cudaStream_t st) {
     if (s & ACE_STATUS_BAD_SPECIES) m += " species out of range;";
     if (s & ACE_STATUS_BAD_POSITION) m += " bad position;";
     if (s & ACE_STATUS_SCRATCH) m += " scratch too small;";
+    if (s & ACE_STATUS_TIMEOUT) m += " tensor-core wait timed out;";
     ctx->err = m;
     cudaMemsetAsync(ctx->d_status, 0, sizeof(int), st);
     cudaStreamSynchronize(st);

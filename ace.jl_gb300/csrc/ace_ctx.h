@@ -15,6 +15,7 @@
 #define ACE_STATUS_BAD_SPECIES 2
 #define ACE_STATUS_BAD_POSITION 4
 #define ACE_STATUS_SCRATCH 8
+#define ACE_STATUS_TIMEOUT 16
 
 struct ace_ctx {
   int device = 0, prec = 0, nsm = 0, smem_optin = 0;
@@ -97,7 +98,8 @@ struct ace_ctx {
   float *d_mlp = nullptr;       // parameters [W1 b1 W2 b2 W3 b3]
   float *d_Rext = nullptr;      // [nNbr][2 C] radial values and r-derivatives
   int64_t rext_cap = 0;         // neighbours d_Rext can hold
-  int mlp_grid_f = 0, mlp_grid_b = 0;
+  int mlp_grid_f = 0, mlp_grid_b = 0, mlp_grid_tc = 0;
+  bool mlp_tc = false;          // tensor-core (BF16) inference of the radial MLP
   size_t mlp_smem_f = 0, mlp_smem_b = 0;
 
   std::vector<void *> allocs;
@@ -118,8 +120,12 @@ int launch_dbasis(ace_ctx *ctx, int64_t nEnv, const int64_t *off_d, const int64_
 int mlp_prepare(ace_ctx *ctx);
 int mlp_forward(ace_ctx *ctx, int64_t nEnv, const int64_t *off, int64_t nNbr, const double *rr, const int32_t *sp,
                 float *R, cudaStream_t st);
+int mlp_infer(ace_ctx *ctx, int64_t nEnv, const int64_t *off, int64_t nNbr, const double *rr, const int32_t *sp,
+              float *R, cudaStream_t st);
+// radial channels of the batch into the context's buffer; infer = false keeps
+// the FP32 MLP (training), true allows the tensor-core inference kernel
 int learned_radials(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const double *rr, const int32_t *sp,
-                    cudaStream_t st);
+                    cudaStream_t st, bool infer = true);
 int launch_radial_adjoint(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const double *rr, const int32_t *sp,
                           double *E, double *G, float *GR, cudaStream_t st);
 int launch_adjoint_eval_d(ace_ctx *ctx, int64_t nEnv, const int64_t *off_d, const int64_t *off_h,

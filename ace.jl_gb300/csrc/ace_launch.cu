@@ -157,7 +157,7 @@ static int ensure_scratch(ace_ctx *ctx, size_t bytes) {
 int launch_radial_adjoint(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const double *rr, const int32_t *sp,
                           double *E, double *G, float *GR, cudaStream_t st) {
   if (nEnv == 0) return ACE_OK;
-  int rc = learned_radials(ctx, nEnv, off, rr, sp, st);
+  int rc = learned_radials(ctx, nEnv, off, rr, sp, st, false);
   if (rc) return rc;
   EFArgs a = make_args(ctx, nEnv, off, rr, sp, E, G);
   a.GR = GR;

@@ -20,7 +20,10 @@
 
 #include <algorithm>
 #include <cmath>
+#include <string>
 #include <vector>
+
+#include <cuda_bf16.h>
 
 #include "../../include/ace_b200.h"
 #include "ace_ctx.h"
@@ -372,6 +375,282 @@ __global__ void adam_kernel(int64_t n, float *w, const float *g, float *m, float
   }
 }
 
+// ---------------------------------------------------------------------------
+// Tensor-core inference: the same MLP with BF16 operands and FP32
+// accumulation on the 5th-generation tensor cores.  One CTA (4 warps) takes
+// 128 neighbours at a time; each layer is two tcgen05.mma GEMMs (values and
+// their t-tangents) of M = 128 rows against the layer's weights, issued by one
+// thread from shared memory into TMEM, completion signalled through an
+// mbarrier; the epilogue reads each thread's row back with tcgen05.ld, applies
+// bias and SiLU (and the tangent chain rule) in FP32 and stores the next
+// layer's BF16 operand.  Operands use the no-swizzle K-major layout: 8-row x
+// 16-byte core matrices, LBO = 128 B between core matrices along K, SBO =
+// K * 16 B between 8-row groups.
+
+constexpr uint32_t TC_COLS = 256;        // TMEM columns per CTA: values at 0, tangents at 128
+constexpr int TC_N3 = 96;                // output channels padded to a multiple of 16
+constexpr int TC_K1 = 16;                // layer-1 inputs padded to one MMA K step
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor: start, leading and stride byte offsets,
+// fixed version bits 46-48 = 0b001, no swizzle
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// instruction descriptor, kind::f16: FP32 accumulator, BF16 A and B, both K-major
+__host__ __device__ constexpr uint32_t umma_idesc(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t dtmem, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dtmem),
+      "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void umma_commit(uint32_t mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+               : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, int64_t limit) {
+  for (int64_t i = 0; i < limit; ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(done)
+        : "r"(mbar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+// 16 consecutive FP32 columns of this warp's 32 TMEM lanes (one row per thread)
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// byte offset of element (row, k) in a K-major no-swizzle operand with K columns
+__device__ __forceinline__ uint32_t kmaj_off(int row, int k, int K) {
+  return (uint32_t)((row >> 3) * (K * 16) + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+  return *(const uint32_t *)&v;
+}
+
+// 8 consecutive k of one row (one core-matrix row, 16 bytes)
+__device__ __forceinline__ void st_row8(unsigned char *base, int row, int k0, int K, const float *x) {
+  uint4 q;
+  q.x = pack_bf16(x[0], x[1]);
+  q.y = pack_bf16(x[2], x[3]);
+  q.z = pack_bf16(x[4], x[5]);
+  q.w = pack_bf16(x[6], x[7]);
+  *(uint4 *)(base + kmaj_off(row, k0, K)) = q;
+}
+
+struct TCSmem {
+  // operands (BF16, K-major core-matrix layout)
+  unsigned char W1[MLP_H * TC_K1 * 2];
+  unsigned char W2[MLP_H * MLP_H * 2];
+  unsigned char W3[TC_N3 * MLP_H * 2];
+  unsigned char X[2][128 * MLP_H * 2];   // [0] F / H2 values, [1] their tangents
+  unsigned char Y[2][128 * MLP_H * 2];   // H1 values, tangents
+  float b1[MLP_H], b2[MLP_H], b3[TC_N3];
+  unsigned long long mbar;
+  uint32_t taddr;
+};
+
+__global__ void __launch_bounds__(128) mlp_fwd_tc_kernel(MLPArgs a) {
+  constexpr int H = MLP_H;
+  extern __shared__ __align__(1024) unsigned char smraw[];
+  TCSmem &S = *(TCSmem *)smraw;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const MLPOff o = mlp_off(H, a.D, a.C);
+  // weights -> BF16 operands (zero padding), biases -> FP32
+  for (int i = tid; i < H * TC_K1; i += 128) {
+    const int n = i / TC_K1, k = i - n * TC_K1;
+    const float w = (k < a.D) ? a.W[o.W1 + n * a.D + k] : 0.f;
+    *(__nv_bfloat16 *)(S.W1 + kmaj_off(n, k, TC_K1)) = __float2bfloat16_rn(w);
+  }
+  for (int i = tid; i < H * H; i += 128) {
+    const int n = i / H, k = i - n * H;
+    *(__nv_bfloat16 *)(S.W2 + kmaj_off(n, k, H)) = __float2bfloat16_rn(a.W[o.W2 + i]);
+  }
+  for (int i = tid; i < TC_N3 * H; i += 128) {
+    const int n = i / H, k = i - n * H;
+    const float w = (n < a.C) ? a.W[o.W3 + (int64_t)n * H + k] : 0.f;
+    *(__nv_bfloat16 *)(S.W3 + kmaj_off(n, k, H)) = __float2bfloat16_rn(w);
+  }
+  for (int i = tid; i < H; i += 128) { S.b1[i] = a.W[o.b1 + i]; S.b2[i] = a.W[o.b2 + i]; }
+  for (int i = tid; i < TC_N3; i += 128) S.b3[i] = (i < a.C) ? a.W[o.b3 + i] : 0.f;
+  const uint32_t mbar = smem_u32(&S.mbar);
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&S.taddr)),
+                 "r"(TC_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = S.taddr;
+  const uint32_t trow = tmem + ((uint32_t)(32 * warp) << 16);  // this warp's lanes
+  const uint32_t i1 = umma_idesc(128, H), i3 = umma_idesc(128, TC_N3);
+  const int64_t limit = int64_t(1) << 26;
+  uint32_t phase = 0;
+  bool ok = true;
+  const int64_t n = a.n >= 0 ? a.n : a.off[a.nEnv];
+
+  // one layer: D_values = X[0] W^T, D_tangents = X[1] W^T over nk K-steps of 16
+  auto issue = [&](unsigned char *const *A, const unsigned char *W, int K, int nk, uint32_t idesc) {
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    if (tid == 0) {
+      tc_fence_after();
+      for (int v = 0; v < 2; ++v)
+        for (int s = 0; s < nk; ++s)
+          umma_bf16(tmem + (uint32_t)(128 * v), umma_desc(smem_u32(A[v]) + 256u * s, 128u, (uint32_t)(K * 16)),
+                    umma_desc(smem_u32(W) + 256u * s, 128u, (uint32_t)(K * 16)), idesc, s > 0 ? 1u : 0u);
+      umma_commit(mbar);
+    }
+    // a wait that gives up leaves the phase pending (waited on again before
+    // the TMEM is freed); the block agrees on the outcome
+    const bool done = __syncthreads_and(mbar_wait(mbar, phase, limit) ? 1 : 0) != 0;
+    if (done) phase ^= 1u;
+    tc_fence_after();
+    return done;
+  };
+
+  for (int64_t base = (int64_t)blockIdx.x * 128; base < n && ok; base += (int64_t)gridDim.x * 128) {
+    const int64_t j = base + tid;
+    const bool act = j < n;
+    float f[MLP_MAXD], df[MLP_MAXQ];
+    const Feat q = mlp_inputs(a, act ? j : n - 1, f, df);
+    {
+      float x[16], dx[16];
+#pragma unroll
+      for (int k = 0; k < 16; ++k) {
+        x[k] = (k < a.D) ? f[k < MLP_MAXD ? k : 0] : 0.f;
+        dx[k] = (k < a.Q) ? df[k < MLP_MAXQ ? k : 0] : 0.f;
+      }
+      st_row8(S.X[0], tid, 0, TC_K1, x);
+      st_row8(S.X[0], tid, 8, TC_K1, x + 8);
+      st_row8(S.X[1], tid, 0, TC_K1, dx);
+      st_row8(S.X[1], tid, 8, TC_K1, dx + 8);
+    }
+    unsigned char *X[2] = {S.X[0], S.X[1]};
+    unsigned char *Y[2] = {S.Y[0], S.Y[1]};
+    if (!issue(X, S.W1, TC_K1, 1, i1)) { ok = false; break; }
+    // layer-1 epilogue -> Y
+#pragma unroll
+    for (int c0 = 0; c0 < H; c0 += 16) {
+      float z[16], dz[16], h[16], dh[16];
+      tmem_ld16(trow + c0, z);
+      tmem_ld16(trow + 128 + c0, dz);
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        const float zz = z[i] + S.b1[c0 + i];
+        const float sg = sigm(zz);
+        h[i] = zz * sg;
+        dh[i] = sg * (1.f + zz * (1.f - sg)) * dz[i];
+      }
+      st_row8(Y[0], tid, c0, H, h);
+      st_row8(Y[0], tid, c0 + 8, H, h + 8);
+      st_row8(Y[1], tid, c0, H, dh);
+      st_row8(Y[1], tid, c0 + 8, H, dh + 8);
+    }
+    if (!issue(Y, S.W2, H, H / 16, i1)) { ok = false; break; }
+    // layer-2 epilogue -> X
+#pragma unroll
+    for (int c0 = 0; c0 < H; c0 += 16) {
+      float z[16], dz[16], h[16], dh[16];
+      tmem_ld16(trow + c0, z);
+      tmem_ld16(trow + 128 + c0, dz);
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        const float zz = z[i] + S.b2[c0 + i];
+        const float sg = sigm(zz);
+        h[i] = zz * sg;
+        dh[i] = sg * (1.f + zz * (1.f - sg)) * dz[i];
+      }
+      st_row8(X[0], tid, c0, H, h);
+      st_row8(X[0], tid, c0 + 8, H, h + 8);
+      st_row8(X[1], tid, c0, H, dh);
+      st_row8(X[1], tid, c0 + 8, H, dh + 8);
+    }
+    if (!issue(X, S.W3, H, H / 16, i3)) { ok = false; break; }
+    // output epilogue: 32 channels at a time staged in the (free) H1 buffers
+    // as [row][R 32 | dR 32] and stored row segment by row segment, 16 bytes
+    // per thread, so a warp writes whole 128-byte lines
+    float *stage = (float *)S.Y[0];
+    const int nrow = (n - base < 128) ? (int)(n - base) : 128;
+    for (int c0 = 0; c0 < TC_N3; c0 += 32) {
+      float ov[32], dv[32];
+      tmem_ld16(trow + c0, *(float(*)[16])ov);
+      tmem_ld16(trow + c0 + 16, *(float(*)[16])(ov + 16));
+      tmem_ld16(trow + 128 + c0, *(float(*)[16])dv);
+      tmem_ld16(trow + 128 + c0 + 16, *(float(*)[16])(dv + 16));
+#pragma unroll
+      for (int i = 0; i < 32; ++i) {
+        const int c = c0 + i;
+        const float y = ov[i] + S.b3[c < TC_N3 ? c : 0];
+        // row-rotated columns keep the staging writes conflict free
+        stage[tid * 64 + ((i + tid) & 31)] = q.fe * y;
+        stage[tid * 64 + 32 + ((i + tid) & 31)] = (q.dfe * y + q.fe * dv[i]) * q.dtdr;
+      }
+      __syncthreads();
+      const int nc = (a.C - c0 < 32) ? a.C - c0 : 32;  // channels of this chunk (a multiple of 4)
+      const int per_row = 2 * (nc / 4);       // float4 pieces of a row: R then dR
+      for (int p = tid; p < nrow * per_row; p += 128) {
+        const int r = p / per_row, w = p - r * per_row;
+        const int half = w >= nc / 4, c4 = (half ? w - nc / 4 : w) * 4;
+        float4 v;
+        const float *src = stage + r * 64 + half * 32;
+        v.x = src[(c4 + 0 + r) & 31];
+        v.y = src[(c4 + 1 + r) & 31];
+        v.z = src[(c4 + 2 + r) & 31];
+        v.w = src[(c4 + 3 + r) & 31];
+        *(float4 *)(a.R + (size_t)(base + r) * 2 * a.C + half * a.C + c0 + c4) = v;
+      }
+      __syncthreads();
+    }
+  }
+  if (!ok) {
+    if (tid == 0) atomicOr(a.status, ACE_STATUS_TIMEOUT);
+    mbar_wait(mbar, phase, limit);  // the MMAs still in flight, bounded
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_COLS) : "memory");
+}
+
 static MLPArgs mlp_args(const ace_ctx *ctx) {
   MLPArgs a{};
   a.W = ctx->d_mlp;
@@ -396,6 +675,23 @@ static size_t bwd_smem(const ace_ctx *ctx) {
 }
 
 int mlp_prepare(ace_ctx *ctx) {
+  // tensor-core inference when the inputs fit one MMA K step (ACE_B200_MLP=fp32: CUDA cores)
+  const char *menv = getenv("ACE_B200_MLP");
+  ctx->mlp_tc = ctx->mlpD <= TC_K1 && ctx->mlpC <= TC_N3 && ctx->mlpC % 4 == 0 &&
+                !(menv && std::string(menv) == "fp32");
+  if (ctx->mlp_tc) {
+    if (cudaFuncSetAttribute(mlp_fwd_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TCSmem)) !=
+        cudaSuccess) {
+      ctx->err = "cudaFuncSetAttribute failed";
+      return ACE_ERR_CUDA;
+    }
+    int ot = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ot, mlp_fwd_tc_kernel, 128, sizeof(TCSmem));
+    // two CTAs per SM: their TC_COLS TMEM columns fill the SM's 512 and their
+    // shared memory (sizeof(TCSmem) each) keeps a third out
+    (void)ot;
+    ctx->mlp_grid_tc = ctx->nsm * 2;
+  }
   ctx->mlp_smem_f = fwd_smem(ctx);
   ctx->mlp_smem_b = bwd_smem(ctx);
   if (ctx->mlp_smem_f > (size_t)ctx->smem_optin || ctx->mlp_smem_b > (size_t)ctx->smem_optin) {
@@ -432,7 +728,7 @@ int mlp_forward(ace_ctx *ctx, int64_t nEnv, const int64_t *off, int64_t nNbr, co
 
 // radial channels of every neighbour of the batch into the context's buffer
 int learned_radials(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const double *rr, const int32_t *sp,
-                    cudaStream_t st) {
+                    cudaStream_t st, bool infer) {
   int64_t nNbr = 0;
   if (cudaMemcpyAsync(&nNbr, off + nEnv, sizeof(int64_t), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
       cudaStreamSynchronize(st) != cudaSuccess) {
@@ -452,7 +748,23 @@ int learned_radials(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const double
     ctx->rext_cap = cap;
   }
   if (nNbr == 0) return ACE_OK;
-  return mlp_forward(ctx, nEnv, off, nNbr, rr, sp, ctx->d_Rext, st);
+  if (!ctx->mlp_tc || !infer) return mlp_forward(ctx, nEnv, off, nNbr, rr, sp, ctx->d_Rext, st);
+  return mlp_infer(ctx, nEnv, off, nNbr, rr, sp, ctx->d_Rext, st);
+}
+
+// inference radials: tensor cores when the context allows them, else FP32
+int mlp_infer(ace_ctx *ctx, int64_t nEnv, const int64_t *off, int64_t nNbr, const double *rr, const int32_t *sp,
+              float *R, cudaStream_t st) {
+  if (!ctx->mlp_tc) return mlp_forward(ctx, nEnv, off, nNbr, rr, sp, R, st);
+  MLPArgs a = mlp_args(ctx);
+  a.n = nNbr; a.off = off; a.nEnv = nEnv; a.rr = rr; a.sp = sp; a.R = R;
+  const int64_t tiles = nNbr >= 0 ? (nNbr + 127) / 128 : ctx->mlp_grid_tc;
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(tiles, ctx->mlp_grid_tc));
+  void *args[] = {&a};
+  cudaError_t e = cudaLaunchKernel((void *)mlp_fwd_tc_kernel, dim3(grid), dim3(128), args, sizeof(TCSmem), st);
+  ctx->launches += 1;
+  if (e != cudaSuccess) { ctx->err = cudaGetErrorString(e); return ACE_ERR_CUDA; }
+  return ACE_OK;
 }
 
 }  // namespace ace
@@ -541,6 +853,16 @@ extern "C" int ace_radial_mlp_forward(ace_ctx *ctx, int64_t nNbr, const double *
   if (ctx->mlpS > 1 && nNbr > 0 && !species) return mfail(ctx, ACE_ERR_INVALID, "species required");
   if (nNbr == 0) return ACE_OK;
   return mlp_forward(ctx, 0, nullptr, nNbr, rr, ctx->mlpS > 1 ? species : nullptr, R, (cudaStream_t)stream);
+}
+
+extern "C" int ace_radial_mlp_infer(ace_ctx *ctx, int64_t nNbr, const double *rr, const int32_t *species, float *R,
+                                    void *stream) {
+  if (!ctx) return ACE_ERR_INVALID;
+  if (!ctx->learned) return mfail(ctx, ACE_ERR_INVALID, "no radial MLP set");
+  if (nNbr < 0 || (nNbr > 0 && (!rr || !R))) return mfail(ctx, ACE_ERR_INVALID, "NULL or negative argument");
+  if (ctx->mlpS > 1 && nNbr > 0 && !species) return mfail(ctx, ACE_ERR_INVALID, "species required");
+  if (nNbr == 0) return ACE_OK;
+  return mlp_infer(ctx, 0, nullptr, nNbr, rr, ctx->mlpS > 1 ? species : nullptr, R, (cudaStream_t)stream);
 }
 
 extern "C" int ace_radial_mlp_backward(ace_ctx *ctx, int64_t nNbr, const double *rr, const int32_t *species,

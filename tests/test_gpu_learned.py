@@ -2,7 +2,8 @@
 
 * the MLP forward (R, dR/dr) and backward (parameter gradient) kernels
   against the FP64 numpy restatement (oracle/mlp_oracle.py): 2e-5 and 1e-4
-  relative to the largest magnitude;
+  relative to the largest magnitude; the tensor-core (BF16) inference kernel
+  within 2e-2 (R) and 4e-2 (dR/dr);
 * energies, forces and the radial adjoint dE/dR of the learned form (FP32)
   against the FP64 C oracle fed the same radial channels: 3e-5 (E), 1e-4
   (dE/drr, dE/dR);
@@ -76,6 +77,14 @@ def test_mlp_forward_backward(lib, student):
     torch.cuda.synchronize()
     gref = mlp_oracle.backward(mlp.params.astype(np.float64), r, b.species, gR, wj, cfg, mlp.C)
     assert relerr(g.cpu().numpy(), gref) <= 1e-4
+    # inference radials on the tensor cores (BF16 operands, FP32 accumulation)
+    Rt = torch.empty_like(R)
+    ctx.radial_mlp_infer(rr, sp, Rt)
+    torch.cuda.synchronize()
+    Rt = Rt.cpu().numpy()
+    print("tensor-core inference: R", relerr(Rt[:, :mlp.C], Rref), "dR", relerr(Rt[:, mlp.C:], dRref))
+    assert relerr(Rt[:, :mlp.C], Rref) <= 2e-2
+    assert relerr(Rt[:, mlp.C:], dRref) <= 4e-2
 
 
 def _oracle_inputs(spec, mlp, b):
@@ -84,8 +93,9 @@ def _oracle_inputs(spec, mlp, b):
     return mlp_oracle.forward(mlp.params.astype(np.float64), r, b.species, mlp.feature_config(spec), mlp.C)
 
 
-def test_learned_energy_forces_and_radial_adjoint(lib, oracle_mod, student):
+def test_learned_energy_forces_and_radial_adjoint(lib, oracle_mod, student, monkeypatch):
     torch = _torch()
+    monkeypatch.setenv("ACE_B200_MLP", "fp32")   # FP32 radials for oracle parity
     spec, mlp = student
     c = random_coefficients(spec, seed=5)
     ctx = learned_context(spec, mlp)
@@ -174,10 +184,11 @@ def test_distillation_gain_and_fallback(lib):
     assert np.allclose(E[ok], Es[ok], rtol=1e-12, atol=0)
 
 
-def test_learned_basis_and_derivative(lib, oracle_mod, student):
+def test_learned_basis_and_derivative(lib, oracle_mod, student, monkeypatch):
     """B and dB of the learned form (FP32) against the oracle fed the same
     radial channels: 1e-5 (B) and 1e-4 (dB) relative to the largest
     magnitude."""
+    monkeypatch.setenv("ACE_B200_MLP", "fp32")
     spec, mlp = student
     ctx = learned_context(spec, mlp)
     b = random_batch(20, 5, 15, nspecies=NS, seed=12)
