@@ -298,6 +298,9 @@ extern "C" int ace_ctx_destroy(ace_ctx *ctx) {
   if (ctx->d_scratch) cudaFree(ctx->d_scratch);
   if (ctx->d_wstage) cudaFree(ctx->d_wstage);
   if (ctx->d_ic_multi) cudaFree(ctx->d_ic_multi);
+  for (cudaStream_t st : {ctx->s_in, ctx->s_comp, ctx->s_out})
+    if (st) cudaStreamDestroy(st);
+  for (cudaEvent_t ev : ctx->pipe_ev) cudaEventDestroy(ev);
   if (ctx->d_mlp) cudaFree(ctx->d_mlp);
   if (ctx->d_Rext) cudaFree(ctx->d_Rext);
   if (ctx->h_status) cudaFreeHost(ctx->h_status);
@@ -413,14 +416,17 @@ extern "C" int ace_set_ctilde(ace_ctx *ctx, const double *ct, int64_t nAA) {
 // learned form (whose spec is single-species)
 static int input_species(const ace_ctx *ctx) { return ctx->learned ? ctx->mlpS : ctx->nspecies; }
 
-static int validate_inputs(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const double *rr,
-                           const int32_t *sp) {
+static int validate_offsets(ace_ctx *ctx, int64_t nEnv, const int64_t *off) {
   if (nEnv < 0) return ctx_fail(ctx, ACE_ERR_INVALID, "nEnv < 0");
   if (off[0] != 0) return ctx_fail(ctx, ACE_ERR_INVALID, "offsets[0] != 0");
   for (int64_t e = 0; e < nEnv; ++e)
     if (off[e + 1] < off[e]) return ctx_fail(ctx, ACE_ERR_INVALID, "offsets not monotone");
-  int64_t n = off[nEnv];
-  for (int64_t j = 0; j < n; ++j) {
+  return ACE_OK;
+}
+
+// positions and species of neighbours [j0, j1)
+static int validate_range(ace_ctx *ctx, int64_t j0, int64_t j1, const double *rr, const int32_t *sp) {
+  for (int64_t j = j0; j < j1; ++j) {
     double x = rr[3 * j], y = rr[3 * j + 1], z = rr[3 * j + 2];
     if (!std::isfinite(x) || !std::isfinite(y) || !std::isfinite(z))
       return ctx_fail(ctx, ACE_ERR_INVALID, "non-finite position");
@@ -430,10 +436,17 @@ static int validate_inputs(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const
   const int nsp = input_species(ctx);
   if (nsp > 1) {
     if (!sp) return ctx_fail(ctx, ACE_ERR_INVALID, "species required for a multi-species spec");
-    for (int64_t j = 0; j < n; ++j)
+    for (int64_t j = j0; j < j1; ++j)
       if (sp[j] < 0 || sp[j] >= nsp) return ctx_fail(ctx, ACE_ERR_INVALID, "species out of range");
   }
   return ACE_OK;
+}
+
+static int validate_inputs(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const double *rr,
+                           const int32_t *sp) {
+  int rc = validate_offsets(ctx, nEnv, off);
+  if (rc) return rc;
+  return validate_range(ctx, 0, off[nEnv], rr, sp);
 }
 
 static int ensure_stage(ace_ctx *ctx, size_t bytes) {
@@ -533,11 +546,88 @@ static int drive(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, const doubl
   return ACE_OK;
 }
 
+// Host buffers in and out, large batches: the batch is cut into chunks of
+// environments; chunk k+1 is validated on the host while chunk k's positions
+// are copied in (copy stream), evaluated (compute stream) and its energies and
+// gradients copied out (a second copy stream), so copies, host checks and
+// kernels overlap.  An invalid chunk stops the pipeline; earlier chunks may
+// then have been evaluated and their outputs written.
+static constexpr int64_t PIPE_MIN_CHUNK = 4096;
+
+static int ensure_pipeline(ace_ctx *ctx, int nchunk) {
+  for (cudaStream_t *p : {&ctx->s_in, &ctx->s_comp, &ctx->s_out})
+    if (!*p) ACE_CUDA(cudaStreamCreateWithFlags(p, cudaStreamNonBlocking));
+  while ((int)ctx->pipe_ev.size() < 2 * nchunk) {
+    cudaEvent_t ev;
+    ACE_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    ctx->pipe_ev.push_back(ev);
+  }
+  return ACE_OK;
+}
+
+static int energy_forces_pipelined(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const double *rr,
+                                   const int32_t *sp, double *E, double *G) {
+  int rc = validate_offsets(ctx, nEnv, off);
+  if (rc) return rc;
+  const int64_t nNbr = off[nEnv];
+  const int nsp = input_species(ctx);
+  if (nsp > 1 && !sp) return ctx_fail(ctx, ACE_ERR_INVALID, "species required for a multi-species spec");
+  const bool wsp = sp && nsp > 1;
+  const int nchunk = (int)std::max<int64_t>(2, std::min<int64_t>(16, nEnv / PIPE_MIN_CHUNK));
+  ACE_CUDA(cudaSetDevice(ctx->device));
+  if ((rc = ensure_pipeline(ctx, nchunk))) return rc;
+  size_t need = 0;
+  const size_t o_off = need; need += al256((nEnv + 1) * sizeof(int64_t));
+  const size_t o_rr = need; need += al256(std::max<int64_t>(nNbr, 1) * 3 * sizeof(double));
+  const size_t o_sp = need; if (wsp) need += al256(std::max<int64_t>(nNbr, 1) * sizeof(int32_t));
+  const size_t o_E = need; need += al256(nEnv * sizeof(double));
+  const size_t o_G = need; if (G) need += al256(std::max<int64_t>(nNbr, 1) * 3 * sizeof(double));
+  if ((rc = ensure_stage(ctx, need))) return rc;
+  char *base = (char *)ctx->d_stage;
+  int64_t *d_off = (int64_t *)(base + o_off);
+  double *d_rr = (double *)(base + o_rr);
+  int32_t *d_sp = wsp ? (int32_t *)(base + o_sp) : nullptr;
+  double *d_E = (double *)(base + o_E);
+  double *d_G = G ? (double *)(base + o_G) : nullptr;
+  ACE_CUDA(cudaMemcpyAsync(d_off, off, (nEnv + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->s_in));
+  int err = ACE_OK;
+  int k = 0;
+  for (; k < nchunk; ++k) {
+    const int64_t e0 = nEnv * k / nchunk, e1 = nEnv * (k + 1) / nchunk;
+    const int64_t j0 = off[e0], j1 = off[e1];
+    if ((err = validate_range(ctx, j0, j1, rr, sp))) break;
+    cudaEvent_t ev_in = ctx->pipe_ev[2 * k], ev_comp = ctx->pipe_ev[2 * k + 1];
+    if (j1 > j0) {
+      ACE_CUDA(cudaMemcpyAsync(d_rr + 3 * j0, rr + 3 * j0, (j1 - j0) * 3 * sizeof(double), cudaMemcpyHostToDevice,
+                               ctx->s_in));
+      if (wsp)
+        ACE_CUDA(cudaMemcpyAsync(d_sp + j0, sp + j0, (j1 - j0) * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->s_in));
+    }
+    ACE_CUDA(cudaEventRecord(ev_in, ctx->s_in));
+    ACE_CUDA(cudaStreamWaitEvent(ctx->s_comp, ev_in, 0));
+    if ((err = launch_energy_forces(ctx, e1 - e0, d_off + e0, d_rr, d_sp, d_E + e0, d_G, ctx->s_comp))) break;
+    ACE_CUDA(cudaEventRecord(ev_comp, ctx->s_comp));
+    ACE_CUDA(cudaStreamWaitEvent(ctx->s_out, ev_comp, 0));
+    ACE_CUDA(cudaMemcpyAsync(E + e0, d_E + e0, (e1 - e0) * sizeof(double), cudaMemcpyDeviceToHost, ctx->s_out));
+    if (G && j1 > j0)
+      ACE_CUDA(cudaMemcpyAsync(G + 3 * j0, d_G + 3 * j0, (j1 - j0) * 3 * sizeof(double), cudaMemcpyDeviceToHost,
+                               ctx->s_out));
+  }
+  ACE_CUDA(cudaStreamSynchronize(ctx->s_out));
+  ACE_CUDA(cudaStreamSynchronize(ctx->s_comp));
+  ACE_CUDA(cudaStreamSynchronize(ctx->s_in));
+  if (err) return err;
+  return read_status(ctx, ctx->s_comp);
+}
+
 extern "C" int ace_energy_forces(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, const double *rr,
                                  const int32_t *species, double *E, double *dEdrr, int32_t flags,
                                  void *stream) {
   if (!ctx) return ACE_ERR_INVALID;
   if (!E) return ctx_fail(ctx, ACE_ERR_INVALID, "E is NULL");
+  if (!(flags & (ACE_INPUTS_ON_DEVICE | ACE_OUTPUTS_ON_DEVICE)) && !ctx->learned && offsets && rr &&
+      nEnv >= 2 * PIPE_MIN_CHUNK)
+    return energy_forces_pipelined(ctx, nEnv, offsets, rr, species, E, dEdrr);
   int64_t nNbr = (flags & ACE_INPUTS_ON_DEVICE) ? 0 : (offsets ? offsets[nEnv] : 0);
   if ((flags & ACE_INPUTS_ON_DEVICE) && dEdrr && !(flags & ACE_OUTPUTS_ON_DEVICE))
     return ctx_fail(ctx, ACE_ERR_INVALID, "host gradient output needs host inputs (the size is unknown)");

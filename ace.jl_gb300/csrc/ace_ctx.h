@@ -102,6 +102,10 @@ struct ace_ctx {
   bool mlp_tc = false;          // tensor-core (BF16) inference of the radial MLP
   size_t mlp_smem_f = 0, mlp_smem_b = 0;
 
+  // host-buffer pipeline (copy in, compute, copy out)
+  cudaStream_t s_in = nullptr, s_comp = nullptr, s_out = nullptr;
+  std::vector<cudaEvent_t> pipe_ev;
+
   std::vector<void *> allocs;
   int64_t launches = 0;
   std::string err;

@@ -342,8 +342,9 @@ def run_learned(args, torch, dist, rank, world, local):
             "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
             "config": {"workload": X["name"], "nenv_per_gpu": nenv, "nnbr_per_gpu": int(ev.nnbr),
-                       "form": "learned radial (MLP 8 Chebyshev + 4 species -> 64 -> 64 -> 8 x 11 channels, "
-                               "FP32) + FP32 Ylm/A/AA/adjoint/forces on the student spec",
+                       "form": "learned radial (MLP 8 Chebyshev + 4 species -> 64 -> 64 -> 8 x 11 channels; "
+                               "FP32 weights, BF16 tcgen05 tensor-core inference GEMMs) + FP32 Ylm/A/AA/adjoint/"
+                               "forces on the student spec",
                        "student": {"maxdeg": sdeg, "K": X["K"], "nA": spec.nA, "nAA": spec.nAA, "nB": spec.nB},
                        "teacher": {"nA": teacher_spec.nA, "nAA": teacher_spec.nAA, "nB": teacher_spec.nB},
                        "l2": "flushed (256 MB write) between timed steps"},
@@ -353,12 +354,13 @@ def run_learned(args, torch, dist, rank, world, local):
                          "force_envs": nf if fw > 0 else 0, "force_weight": fw,
                          "pretrain_s": t1 - t0, "distill_s": t2 - t1, "setup_s": t0 - t_setup,
                          "loss_first_last": [hist[0], hist[-1]] if hist else None},
-            "forms": {"learned_fp32": {"value": value},
+            "forms": {"learned": {"value": value},
                       "plain_fp64": {"value": 2 * n64 / t64, "envs": n64},
                       "plain_fp32x2": {"value": nenv / tx2}},
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peaks["fp32_tflops"], "unit": "TFLOP/s",
                          "frac": achieved / peaks["fp32_tflops"], "traffic": None,
-                         "kernel": "mlp_fwd_kernel + ef_kernel<float> (learned radial form)",
+                         "kernel": "mlp_fwd_tc_kernel + ef_kernel<float> (learned radial form); MLP flops counted "
+                                   "with the FP32 CUDA-core ones",
                          "flops_per_env": fl / nenv},
             "clocks": clk.summary(), "gpu_launches": int(launches), "peaks_measured": peaks}
     print(json.dumps(line), flush=True)

@@ -384,3 +384,36 @@ def test_full_size_order4_degree12(lib, oracle_mod):
     Ep, Gp = cx2.energy_forces(b.offsets, b.rr[perm])
     assert energy_relerr(Ep, E) <= 1e-6
     assert relerr(Gp, G[perm]) <= 1e-4
+
+
+def test_host_pipeline(lib, oracle_mod):
+    """Large host-buffer calls run as a chunked copy/compute pipeline: the
+    results equal the device-pointer call, and an invalid position in a late
+    chunk is still reported."""
+    torch = pytest.importorskip("torch")
+    spec = get_spec("test")
+    c = random_coefficients(spec, seed=3)
+    ctx = lib.Context(spec, "fp64")
+    ctx.set_params(c)
+    b = random_batch(20000, 4, 12, seed=17)
+    E, G = ctx.energy_forces(b.offsets, b.rr)
+    dev = torch.device("cuda", 0)
+    off_d = torch.from_numpy(b.offsets).to(dev)
+    rr_d = torch.from_numpy(b.rr).to(dev)
+    Ed = torch.empty(b.nenv, dtype=torch.float64, device=dev)
+    Gd = torch.empty_like(rr_d)
+    ctx.energy_forces_device(off_d, rr_d, None, Ed, Gd)
+    assert np.array_equal(E, Ed.cpu().numpy())
+    assert np.allclose(G, Gd.cpu().numpy(), rtol=1e-12, atol=1e-15)
+    idx = np.random.default_rng(0).choice(b.nenv, 50, replace=False)
+    off = np.concatenate([[0], np.cumsum(np.diff(b.offsets)[idx])])
+    rr = np.concatenate([b.rr[b.offsets[e]:b.offsets[e + 1]] for e in idx])
+    Eo, Go = oracle_mod.Oracle(spec, c).energy_forces(off, rr)
+    assert energy_relerr(E[idx], Eo) <= 1e-12
+    bad = b.rr.copy()
+    bad[b.offsets[19990]] = np.nan
+    with pytest.raises(lib.AceError):
+        ctx.energy_forces(b.offsets, bad)
+    # the context stays usable
+    E2, _ = ctx.energy_forces(b.offsets, b.rr)
+    assert np.array_equal(E2, E)
