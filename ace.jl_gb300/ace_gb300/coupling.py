@@ -223,3 +223,138 @@ def rpe_basis(ll: tuple, pattern: tuple) -> np.ndarray:
         return np.zeros((0, mm.shape[0]))
     rk = int(np.sum(S > 1e-7 * S[0]))
     return np.diag(np.sqrt(S[:rk])) @ U[:, :rk].T @ Ure
+
+
+# ---------------------------------------------------------------------------
+# Equivariant vector (EuclideanVector) couplings, src/properties.jl:154-248.
+#
+# The coupling tree above, ended in total angular momentum L instead of 0,
+# gives rows T_J(mm) over the m-tuples with |sum mm| <= L; for L = 1 each row
+# defines a spherical vector F_M = sum_{sum mm = M} T_J(mm) prod Y_{l_t m_t}
+# that rotates like Y_1^M.  With Y_1^{-1} = (x - iy)/sqrt2, Y_1^0 = z,
+# Y_1^{+1} = -(x + iy)/sqrt2 (up to a common factor, Condon-Shortley phase),
+# the Cartesian components are x = (F_{-1} - F_{+1})/sqrt2,
+# y = i (F_{-1} + F_{+1})/sqrt2, z = F_0.  Their real and imaginary parts
+# are real O(3)-equivariant vector functions (for odd sum(ll)); a real
+# function is represented by coefficients u with u(mm) = (-1)^{sum mm}
+# conj(u(-mm)), for which sum_mm u(mm) AA(mm) is real.
+
+
+@lru_cache(maxsize=None)
+def mrange_L(ll: tuple, L: int) -> np.ndarray:
+    """All mm with |m_t| <= l_t and |sum(mm)| <= L, in CartesianIndices order."""
+    N = len(ll)
+    if N == 0:
+        return np.zeros((0, 0), dtype=np.int64)
+    grids = np.meshgrid(*[np.arange(-l, l + 1) for l in ll], indexing="ij")
+    mm = np.stack([g.ravel(order="F") for g in grids], axis=1)
+    return mm[np.abs(mm.sum(axis=1)) <= L].astype(np.int64)
+
+
+@lru_cache(maxsize=None)
+def coupling_tree_L(ll: tuple, L: int) -> np.ndarray:
+    """Rows T_J(mm) over ``mrange_L(ll, L)``: coupling paths as in
+    ``coupling_tree`` whose last step couples l_1 with j_2 into L (M = sum mm)."""
+    mm = mrange_L(ll, L)
+    N = len(ll)
+    nM = mm.shape[0]
+    if nM == 0:
+        return np.zeros((0, 0))
+    if N == 1:
+        return np.ones((1, nM)) if ll[0] == L else np.zeros((0, nM))
+    Mcur = mm[:, N - 1].copy()
+    states = [(ll[N - 1], np.ones(nM))]
+    for s in range(N - 2, -1, -1):
+        ls = ll[s]
+        ms = mm[:, s]
+        Mnew = Mcur + ms
+        new_states = []
+        for (j, coef) in states:
+            if s == 0:
+                jrange = [L] if abs(ls - j) <= L <= ls + j else []
+            else:
+                jrange = range(abs(ls - j), ls + j + 1)
+            for jn in jrange:
+                tab = _cg_table(ls, j, jn)
+                ok = np.abs(Mnew) <= jn
+                c = np.where(ok, tab[ms + ls, np.clip(Mcur + j, 0, 2 * j)], 0.0)
+                c = np.where(np.abs(Mcur) <= j, c, 0.0)
+                cn = coef * c
+                if np.any(cn != 0):
+                    new_states.append((jn, cn))
+        states = new_states
+        Mcur = Mnew
+    if not states:
+        return np.zeros((0, nM))
+    return np.stack([c for (_, c) in states], axis=0)
+
+
+def _neg_index(mm: np.ndarray, ll: tuple) -> np.ndarray:
+    """Index of -mm for every row of mm (the set is closed under negation)."""
+    N = len(ll)
+    lmax = max(ll)
+    base = 2 * lmax + 1
+    w = base ** np.arange(N)
+    keys = ((mm + lmax) * w).sum(axis=1)
+    order = np.argsort(keys)
+    nk = ((-mm + lmax) * w).sum(axis=1)
+    return order[np.searchsorted(keys[order], nk)]
+
+
+def _real_rows(G: np.ndarray, neg: np.ndarray, sgn: np.ndarray) -> np.ndarray:
+    """(G + sigma(G))/2 with sigma(G)(mm) = (-1)^{sum mm} conj(G(-mm)); G is
+    (..., 3, nM)."""
+    return 0.5 * (G + sgn * np.conj(G[..., neg]))
+
+
+@lru_cache(maxsize=None)
+def vector_rpe_basis(ll: tuple, pattern: tuple) -> np.ndarray:
+    """Coefficients (nb, 3, nM) over ``mrange_L(ll, 1)`` of an independent,
+    permutation-symmetrised set of real equivariant vector functions of one
+    (nn, ll) class (the role of src/symmetrygroups.jl:119-146 for
+    EuclideanVector): real and imaginary parts of every coupling path's
+    Cartesian vector, reduced to a basis by an SVD (rank rtol 1e-7), then
+    the permutation Gramian over the stabiliser of (nn, ll), SVD and rank
+    rtol 1e-7 as in ``rpe_basis``."""
+    mm = mrange_L(ll, 1)
+    nM = mm.shape[0]
+    T = coupling_tree_L(ll, 1)
+    if T.shape[0] == 0 or nM == 0:
+        return np.zeros((0, 3, nM), dtype=complex)
+    M = mm.sum(axis=1)
+    s2 = 1.0 / np.sqrt(2.0)
+    cart = np.zeros((3, nM), dtype=complex)      # F_i = sum_M cart[i, M] F_M, per mm
+    cart[0] = np.where(M == -1, s2, 0.0) - np.where(M == 1, s2, 0.0)
+    cart[1] = 1j * (np.where(M == -1, s2, 0.0) + np.where(M == 1, s2, 0.0))
+    cart[2] = np.where(M == 0, 1.0, 0.0)
+    G = T[:, None, :] * cart[None, :, :]         # (npath, 3, nM)
+    neg = _neg_index(mm, ll)
+    sgn = np.where(M % 2 == 0, 1.0, -1.0)
+    rows = np.concatenate([_real_rows(G, neg, sgn), _real_rows(-1j * G, neg, sgn)], axis=0)
+    R = np.concatenate([rows.real.reshape(len(rows), -1), rows.imag.reshape(len(rows), -1)], axis=1)
+    _, S, Vh = np.linalg.svd(R, full_matrices=False)
+    if S.size == 0 or S[0] <= 0:
+        return np.zeros((0, 3, nM), dtype=complex)
+    W = Vh[:int(np.sum(S > 1e-7 * S[0]))]          # orthonormal real rows (re | im)
+    # permutation Gramian
+    N = len(ll)
+    lmax = max(ll)
+    base = 2 * lmax + 1
+    w = base ** np.arange(N)
+    keys = ((mm + lmax) * w).sum(axis=1)
+    order = np.argsort(keys)
+    skeys = keys[order]
+    half = 3 * nM
+    Gm = np.zeros((len(W), len(W)))
+    for sig in stabiliser(pattern, ll):
+        pk = ((mm[:, list(sig)] + lmax) * w).sum(axis=1)
+        idx = order[np.searchsorted(skeys, pk)]
+        full = np.concatenate([(np.arange(3)[:, None] * nM + idx[None, :]).ravel(),
+                               half + (np.arange(3)[:, None] * nM + idx[None, :]).ravel()])
+        Gm += W @ W[:, full].T
+    U, S, _ = np.linalg.svd(Gm)
+    if S.size == 0 or S[0] <= 0:
+        return np.zeros((0, 3, nM), dtype=complex)
+    rk = int(np.sum(S > 1e-7 * S[0]))
+    Wr = np.diag(np.sqrt(S[:rk])) @ U[:, :rk].T @ W
+    return (Wr[:, :half] + 1j * Wr[:, half:]).reshape(rk, 3, nM)

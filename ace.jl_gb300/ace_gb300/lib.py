@@ -26,7 +26,8 @@ EXPORTED = ("ace_ctx_create", "ace_ctx_destroy", "ace_set_params", "ace_set_ctil
             "ace_last_error_string", "ace_launch_count", "ace_basis_noalloc", "ace_adjoint_eval_d",
             "ace_set_params_multi", "ace_energy_forces_multi", "ace_autotune", "ace_set_radial_mlp",
             "ace_radial_mlp_params", "ace_radial_mlp_forward", "ace_radial_mlp_backward",
-            "ace_energy_radial_adjoint", "ace_adam_step", "ace_radial_mlp_get_params", "ace_radial_mlp_infer")
+            "ace_energy_radial_adjoint", "ace_adam_step", "ace_radial_mlp_get_params", "ace_radial_mlp_infer",
+            "ace_set_ctilde_complex")
 
 
 class AceError(RuntimeError):
@@ -84,6 +85,7 @@ def load(path: str | None = None):
     lib.ace_radial_mlp_forward.argtypes = [P, C.c_int64, P, P, P, P]
     lib.ace_radial_mlp_get_params.argtypes = [P, P, C.c_int32]
     lib.ace_radial_mlp_infer.argtypes = [P, C.c_int64, P, P, P, P]
+    lib.ace_set_ctilde_complex.argtypes = [P, P, C.c_int64, C.c_int32]
     lib.ace_radial_mlp_backward.argtypes = [P, C.c_int64, P, P, P, P, P, P]
     lib.ace_energy_radial_adjoint.argtypes = [P, C.c_int64, P, P, P, P, P, P, P]
     lib.ace_adam_step.argtypes = [C.c_int64, P, P, P, P, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int32, P]
@@ -99,7 +101,7 @@ def load(path: str | None = None):
             "ace_set_params_multi", "ace_energy_forces_multi", "ace_autotune", "ace_set_radial_mlp",
                  "ace_radial_mlp_params", "ace_radial_mlp_forward", "ace_radial_mlp_backward",
                  "ace_energy_radial_adjoint", "ace_adam_step", "ace_radial_mlp_get_params",
-                 "ace_radial_mlp_infer"):
+                 "ace_radial_mlp_infer", "ace_set_ctilde_complex"):
         getattr(lib, name).restype = C.c_int
     _lib = lib
     return lib
@@ -144,7 +146,7 @@ def make_bundle(spec):
     b.nspecies = spec.nspecies
     b.nAA, b.maxord = spec.nAA, spec.maxorder
     b.orders, b.iAA2iA = _ptr(keep["orders"]), _ptr(keep["iAA2iA"])
-    b.nB = spec.nB
+    b.nB = U.shape[0]
     b.U_indptr, b.U_indices, b.U_data = _ptr(keep["U_indptr"]), _ptr(keep["U_indices"]), _ptr(keep["U_data"])
     return b, keep
 
@@ -235,6 +237,13 @@ class Context:
         cm = np.ascontiguousarray(c.T)
         self.nprop = cm.shape[0]
         self._check(self.lib.ace_set_params_multi(self.h, _ptr(cm), cm.shape[1], cm.shape[0]))
+
+    def set_ctilde_complex(self, ct):
+        """ct: complex (nprop, nAA); property p evaluates Re(sum_k ct[p, k] AA_k)."""
+        ct = np.atleast_2d(np.asarray(ct, dtype=np.complex128))
+        buf = np.ascontiguousarray(np.stack([ct.real, ct.imag], axis=-1))
+        self._check(self.lib.ace_set_ctilde_complex(self.h, _ptr(buf), ct.shape[1], ct.shape[0]))
+        self.nprop = ct.shape[0]
 
     def energy_forces_multi(self, offsets, rr, species=None):
         """E (nEnv, nprop) and dE/drr (nNbr, nprop, 3)."""

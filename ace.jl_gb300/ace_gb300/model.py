@@ -158,4 +158,36 @@ class LinearACEModel:
         return self.basis.evaluate_d(cfgs)
 
 
-__all__ = ["ACEConfig", "SymmetricBasis", "LinearACEModel", "random_coefficients", "symmetric_basis"]
+class LinearVectorModel:
+    """A linear model over an EuclideanVector basis (``spec.vector_basis``):
+    V(cfg) = sum_b c_b B_b(cfg) in R^3 (src/properties.jl:154-248 with
+    src/linearmodel.jl's evaluate / grad_config).  Evaluated as three
+    complex-coefficient properties (x, y, z) on the GPU."""
+
+    def __init__(self, spec, c, precision: str = "fp64", device: int = 0):
+        self.spec = spec
+        self.c = np.array(c, dtype=np.float64)
+        self.ctx = Context(spec, precision, device)
+        self.set_params(self.c)
+
+    def set_params(self, c):
+        self.c[...] = c
+        self.ctx.set_ctilde_complex(self.spec.ctilde_vector(self.c))
+        return self
+
+    def evaluate(self, cfgs):
+        """V (3,) per configuration."""
+        single, off, rr, sp = _pack(cfgs)
+        E, _ = self.ctx.energy_forces_multi(off, rr, sp)      # (nEnv, 3)
+        return E[0] if single else E
+
+    def grad_config(self, cfgs):
+        """dV_i/drr_j[a] as (J, 3, 3) (i = component, a = coordinate) per configuration."""
+        single, off, rr, sp = _pack(cfgs)
+        _, G = self.ctx.energy_forces_multi(off, rr, sp)      # (nNbr, 3, 3)
+        parts = [G[off[e]:off[e + 1]] for e in range(len(off) - 1)]
+        return parts[0] if single else parts
+
+
+__all__ = ["ACEConfig", "SymmetricBasis", "LinearACEModel", "LinearVectorModel", "random_coefficients",
+           "symmetric_basis"]

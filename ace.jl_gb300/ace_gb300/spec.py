@@ -75,16 +75,21 @@ def init1pspec(nR: int, maxL: int, maxdeg: float, nspecies: int = 1) -> OnePSpec
 
 
 def gensparse_ordered(deg: np.ndarray, ls: np.ndarray, ms: np.ndarray,
-                      maxorder: int, maxdeg: float) -> list:
+                      maxorder: int, maxdeg: float, prop: str = "invariant") -> list:
     """All ascending tuples v_1 <= ... <= v_k (0-based A indices, k = 0..maxorder)
-    with sum(deg[v]) <= maxdeg, kept when k <= 1 or (sum l even and sum m == 0).
+    with sum(deg[v]) <= maxdeg, kept when k <= 1 or (sum l even and sum m == 0)
+    for the Invariant property (src/properties.jl:133-150), or when sum l is
+    odd and |sum m| <= 1 (k >= 1, no constant) for EuclideanVector
+    (src/properties.jl:189-203,240-246).
     Returned per order k as int arrays (N_k, k), each in lexicographic order,
     which is gensparse's enumeration order (order-major because shorter
     tuples are padded with leading zeros)."""
     deg = np.asarray(deg)
     assert np.all(np.diff(deg) >= 0), "A spec must be sorted by degree"
     nA = len(deg)
-    out = [np.zeros((1, 0), dtype=np.int64)]  # order 0: the constant
+    vec = prop == "vector"
+    mslack = 1 if vec else 0
+    out = [np.zeros((0 if vec else 1, 0), dtype=np.int64)]  # order 0: the constant (invariants only)
     for k in range(1, maxorder + 1):
         # rows: partial tuples, their degree sum and m sum
         tup = np.zeros((1, 0), dtype=np.int64)
@@ -110,9 +115,11 @@ def gensparse_ordered(deg: np.ndarray, ls: np.ndarray, ms: np.ndarray,
             keep = dsum <= maxdeg + 1e-12
             if t < k - 1:
                 # prune: the remaining entries have |m| <= l <= deg <= maxdeg - dsum
-                keep &= np.abs(msum) <= (maxdeg - dsum) + 1e-12
+                keep &= np.abs(msum) <= (maxdeg - dsum) + mslack + 1e-12
             tup, dsum, msum, lsum = tup[keep], dsum[keep], msum[keep], lsum[keep]
-        if k >= 2 and len(tup):
+        if vec and len(tup):
+            tup = tup[(lsum % 2 == 1) & (np.abs(msum) <= 1)]
+        elif k >= 2 and len(tup):
             keep = (lsum % 2 == 0) & (msum == 0)
             tup = tup[keep]
         if len(tup):
@@ -279,6 +286,119 @@ def symmetric_basis(maxorder: int, maxdeg: float, nR: int | None = None,
     return ACESpec(radial=radial, maxL=maxL, nspecies=nspecies, aspec=aspec,
                    orders=orders, iAA2iA=iAA2iA, U=U,
                    Bdeg=np.array(Bdeg), Bclass=np.array(Bclass), info=info)
+
+
+@dataclass
+class VectorSpec(ACESpec):
+    """An EuclideanVector basis: B_b = Re(sum_k U[b, k] AA_k) in R^3, with
+    Uvec = (U_x, U_y, U_z) complex CSR (nB x nAA).  ``U`` (real, used by the
+    invariant paths) is empty; ``nB`` counts vector basis functions."""
+    Uvec: tuple = ()
+
+    @property
+    def nB(self):
+        return self.Uvec[0].shape[0]
+
+    def ctilde_vector(self, c: np.ndarray) -> np.ndarray:
+        """c~^(i) = U_i^T c for i = x, y, z: complex (3, nAA)."""
+        c = np.asarray(c, dtype=np.float64)
+        return np.stack([np.asarray(Ui.T @ c).ravel() for Ui in self.Uvec])
+
+
+def vector_basis(maxorder: int, maxdeg: float, nR: int | None = None, maxL: int | None = None,
+                 nspecies: int = 1, r0: float = 1.0, rcut: float = 5.0, rin: float | None = None,
+                 pcut: int = 2, pin: int = 0, p: int = 2, zero_tol: float = 1e-12) -> VectorSpec:
+    """SymmetricBasis(EuclideanVector(), [Categorical *] RnYlm_1pbasis(maxdeg, maxL),
+    SimpleSparseBasis(maxorder, maxdeg)): rotation-equivariant vector basis
+    functions (src/properties.jl:154-248), built class by class from the
+    coupling tree ended in L = 1 (``coupling.vector_rpe_basis``), cleaned as
+    ``symmetric_basis`` cleans.  The orthonormal basis within a class is the
+    coupling-tree one, not the reference's SVD rotation (parity unpinned, as
+    for invariants)."""
+    from .coupling import mrange_L, vector_rpe_basis
+    if nR is None:
+        nR = int(maxdeg)
+    if maxL is None:
+        maxL = int(maxdeg)
+    radial = rn_basis(maxdeg=nR, r0=r0, rcut=rcut, rin=rin, pcut=pcut, pin=pin, p=p)
+    aspec = init1pspec(nR, maxL, maxdeg, nspecies)
+    nA0 = len(aspec)
+    per_order = gensparse_ordered(aspec.degree.astype(np.float64), aspec.l, aspec.m, maxorder, maxdeg,
+                                  prop="vector")
+    rows, orders = [], []
+    for k, tup in enumerate(per_order):
+        if len(tup) == 0:
+            continue
+        r = -np.ones((len(tup), maxorder), dtype=np.int64)
+        r[:, :k] = tup[:, ::-1]
+        rows.append(r)
+        orders.append(np.full(len(tup), k, dtype=np.int64))
+    iAA2iA = np.concatenate(rows, axis=0)
+    orders = np.concatenate(orders)
+    nAA0 = len(orders)
+    base = nA0 + 1
+    keys = _encode(iAA2iA, base)
+    korder = np.argsort(keys)
+    skeys = keys[korder]
+    aidx = -np.ones((nspecies, nR + 1, maxL + 1, 2 * maxL + 1), dtype=np.int64)
+    aidx[aspec.mu, aspec.n, aspec.l, aspec.m + maxL] = np.arange(nA0)
+    a_m = aspec.m
+    refmask = np.all(np.where(iAA2iA >= 0, a_m[np.maximum(iAA2iA, 0)] == 0, True), axis=1)
+    Irow, Jcol, vals, Bdeg, Bclass = [], [], [], [], []
+    nB = 0
+    nclass = 0
+    for iAA in np.nonzero(refmask)[0]:
+        k = int(orders[iAA])
+        vs = iAA2iA[iAA, :k]
+        ll = tuple(int(x) for x in aspec.l[vs])
+        nn = tuple((int(a), int(b)) for a, b in zip(aspec.mu[vs], aspec.n[vs]))
+        U = vector_rpe_basis(ll, _nn_pattern(nn))          # (nb, 3, nM)
+        if U.shape[0] == 0:
+            continue
+        mm = mrange_L(ll, 1)
+        A = np.stack([aidx[aspec.mu[vs[t]], aspec.n[vs[t]], ll[t], mm[:, t] + maxL] for t in range(k)], axis=1)
+        if np.any(A < 0):
+            raise RuntimeError("m-tuple outside the 1p basis")
+        A = -np.sort(-A, axis=1)
+        r = -np.ones((len(A), maxorder), dtype=np.int64)
+        r[:, :k] = A
+        pk = _encode(r, base)
+        pos = np.searchsorted(skeys, pk)
+        if np.any(pos >= len(skeys)) or np.any(skeys[np.minimum(pos, len(skeys) - 1)] != pk):
+            raise RuntimeError("bcol_ordered not in AA-spec")
+        cols = korder[pos]
+        ucols, inv = np.unique(cols, return_inverse=True)
+        Uc = np.zeros((U.shape[0], 3, len(ucols)), dtype=complex)
+        for i in range(3):
+            np.add.at(Uc[:, i, :].T, inv, U[:, i, :].T)
+        rmax = np.abs(Uc).max(axis=(1, 2), keepdims=True)
+        Uc[np.abs(Uc) <= zero_tol * rmax] = 0.0
+        d = float(sum(aspec.degree[vs]))
+        for irow in range(U.shape[0]):
+            nzm = np.any(Uc[irow] != 0, axis=0)
+            Irow.append(np.full(int(nzm.sum()), nB)); Jcol.append(ucols[nzm]); vals.append(Uc[irow][:, nzm])
+            Bdeg.append(d); Bclass.append(nclass)
+            nB += 1
+        nclass += 1
+    Irow = np.concatenate(Irow); Jcol = np.concatenate(Jcol); V = np.concatenate(vals, axis=1)
+    Ufull = [sp.csr_matrix((V[i], (Irow, Jcol)), shape=(nB, nAA0)) for i in range(3)]
+    colnorm = sum(np.asarray(abs(Ui).sum(axis=0)).ravel() for Ui in Ufull)
+    Inz = np.nonzero(colnorm > 0.0)[0]
+    Uvec = tuple(Ui[:, Inz].tocsr() for Ui in Ufull)
+    iAA2iA = iAA2iA[Inz]
+    orders = orders[Inz]
+    used = np.zeros(nA0, dtype=bool)
+    used[iAA2iA[iAA2iA >= 0]] = True
+    new_inds = -np.ones(nA0, dtype=np.int64)
+    new_inds[used] = np.arange(used.sum())
+    iAA2iA = np.where(iAA2iA >= 0, new_inds[np.maximum(iAA2iA, 0)], -1)
+    aspec = OnePSpec(aspec.mu[used], aspec.n[used], aspec.l[used], aspec.m[used])
+    info = dict(nA_pre=nA0, nAA_pre=nAA0, nclass=nclass, prop="vector",
+                nAA_by_order={int(k): int((orders == k).sum()) for k in np.unique(orders)},
+                maxorder=maxorder, maxdeg=maxdeg, nR=nR, maxL=maxL, nspecies=nspecies)
+    return VectorSpec(radial=radial, maxL=maxL, nspecies=nspecies, aspec=aspec, orders=orders, iAA2iA=iAA2iA,
+                      U=sp.csr_matrix((0, len(orders))), Bdeg=np.array(Bdeg), Bclass=np.array(Bclass), info=info,
+                      Uvec=Uvec)
 
 
 def random_coefficients(spec: ACESpec, seed: int = 0) -> np.ndarray:

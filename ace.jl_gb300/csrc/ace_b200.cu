@@ -184,6 +184,8 @@ extern "C" int ace_ctx_create(const ace_spec_bundle *s, int32_t prec, int32_t de
     Interleaved il = interleave(sch, ctx->nt);
     ctx->sn = sch.n;
     ctx->halved = sch.halved;
+    ctx->apartner = sch.partner;
+    ctx->amsign = sch.msign;
     ctx->sched_nodes = sch.nodes;
     ctx->slen = il.len;
     const int64_t nslot = std::max<int64_t>(il.len * ctx->nt, 1);
@@ -377,6 +379,7 @@ extern "C" int ace_set_params_multi(ace_ctx *ctx, const double *c, int64_t nB, i
   if (nprop < 1 || nprop > 4096) return ctx_fail(ctx, ACE_ERR_INVALID, "nprop out of range [1, 4096]");
   if (!ctx->use_items) return ctx_fail(ctx, ACE_ERR_UNSUPPORTED, "multi-property models need the item schedule");
   ACE_CUDA(cudaSetDevice(ctx->device));
+  ctx->cplx = false;
   ctx->ctilde_multi.assign((size_t)nprop * ctx->nAA, 0.0);
   for (int p = 0; p < nprop; ++p) {
     double *ct = ctx->ctilde_multi.data() + (size_t)p * ctx->nAA;
@@ -398,6 +401,47 @@ extern "C" int ace_set_params_multi(ace_ctx *ctx, const double *c, int64_t nB, i
     int rc = pack_coefs(ctx, (char *)ctx->d_ic_multi + p * per, (int64_t)ctx->ik.size(), [&](int64_t j) {
       return ctx->ik[j] < 0 ? 0.0 : ctx->iw[j] * ct[ctx->ik[j]];
     });
+    if (rc) return rc;
+  }
+  return ACE_OK;
+}
+
+extern "C" int ace_set_ctilde_complex(ace_ctx *ctx, const double *ct, int64_t nAA, int32_t nprop) {
+  if (!ctx || !ct) return ctx_fail(ctx, ACE_ERR_INVALID, "NULL argument");
+  if (nAA != ctx->nAA) return ctx_fail(ctx, ACE_ERR_INVALID, "length of ctilde != nAA");
+  if (nprop < 1 || nprop > 4096) return ctx_fail(ctx, ACE_ERR_INVALID, "nprop out of range [1, 4096]");
+  if (!ctx->use_items) return ctx_fail(ctx, ACE_ERR_UNSUPPORTED, "complex coefficients need the item schedule");
+  ACE_CUDA(cudaSetDevice(ctx->device));
+  const size_t csz = (ctx->prec == ACE_PREC_FP64 || ctx->prec == ACE_PREC_FP32X2) ? 8 : 4;
+  const int64_t ns = (int64_t)ctx->ik.size();
+  const size_t per = 2 * (size_t)ns * csz;
+  if (ctx->d_ic_multi && (nprop > ctx->nprop || !ctx->cplx)) {
+    cudaFree(ctx->d_ic_multi);
+    ctx->d_ic_multi = nullptr;
+  }
+  if (!ctx->d_ic_multi && cudaMalloc(&ctx->d_ic_multi, per * nprop) != cudaSuccess)
+    return ctx_fail(ctx, ACE_ERR_ALLOC, "coefficient allocation failed");
+  ctx->cplx = true;
+  ctx->nprop = nprop;
+  ctx->ctilde_multi.assign((size_t)nprop * ctx->nAA, 0.0);
+  for (int p = 0; p < nprop; ++p) {
+    const double *cp = ct + (size_t)p * 2 * nAA;
+    for (int64_t k = 0; k < nAA; ++k) ctx->ctilde_multi[(size_t)p * nAA + k] = cp[2 * k];
+    // a slot of weight 2 stands for k and its m-reversed partner k':
+    // Re(c_k AA_k + c_k' AA_k') = Re((c_k + s_k conj(c_k')) AA_k)
+    auto coef = [&](int64_t j, bool im) {
+      const int64_t k = ctx->ik[j];
+      if (k < 0) return 0.0;
+      double re = cp[2 * k], ii = cp[2 * k + 1];
+      if (ctx->iw[j] == 2) {
+        const int64_t q = ctx->apartner[k];
+        re += ctx->amsign[k] * cp[2 * q];
+        ii -= ctx->amsign[k] * cp[2 * q + 1];
+      }
+      return im ? ii : re;
+    };
+    int rc = pack_coefs(ctx, (char *)ctx->d_ic_multi + p * per, 2 * ns,
+                        [&](int64_t j) { return j < ns ? coef(j, false) : coef(j - ns, true); });
     if (rc) return rc;
   }
   return ACE_OK;
@@ -656,7 +700,8 @@ extern "C" int ace_energy_forces_multi(ace_ctx *ctx, int64_t nEnv, const int64_t
   }
   const int np = ctx->nprop;
   const size_t csz = (ctx->prec == ACE_PREC_FP64 || ctx->prec == ACE_PREC_FP32X2) ? 8 : 4;
-  const size_t per = ctx->ik.size() * csz;
+  const size_t per = (ctx->cplx ? 2 : 1) * ctx->ik.size() * csz;
+  if (!ctx->use_items) return ctx_fail(ctx, ACE_ERR_UNSUPPORTED, "multi-property models need the item schedule");
   std::vector<std::pair<void *, size_t>> outs = {{E, (size_t)np * nEnv * sizeof(double)},
                                                  {dEdrr, (size_t)np * nNbr * 3 * sizeof(double)}};
   return drive(ctx, nEnv, offsets, rr, species, flags, stream, outs,
@@ -665,7 +710,8 @@ extern "C" int ace_energy_forces_multi(ace_ctx *ctx, int64_t nEnv, const int64_t
                    const double c0 = ctx->has_const ? ctx->ctilde_multi[(size_t)p * ctx->nAA] : 0.0;
                    double *Ep = (double *)d[0] + (size_t)p * nEnv;
                    double *Gp = d[1] ? (double *)d[1] + (size_t)p * nNbr * 3 : nullptr;
-                   int rc = launch_energy_forces(ctx, nEnv, o, x, s, Ep, Gp, st, (char *)ctx->d_ic_multi + p * per, c0);
+                   int rc = launch_energy_forces(ctx, nEnv, o, x, s, Ep, Gp, st, (char *)ctx->d_ic_multi + p * per, c0,
+                                                 ctx->cplx);
                    if (rc) return rc;
                  }
                  return (int)ACE_OK;

@@ -55,7 +55,11 @@ struct ace_ctx {
   void *d_ic = nullptr;        // [(G+1) * item_n] coefficients in the energy type
   std::vector<int64_t> ik;     // [(G+1) * item_n] AA index (-1: none)
   std::vector<uint8_t> iw;     // weights
-  // multi-property coefficient sets (property-major)
+  // multi-property coefficient sets (property-major); cplx: complex c~
+  // (EuclideanVector components), item coefficients in two planes
+  bool cplx = false;
+  std::vector<int64_t> apartner;   // AA partner (halved schedules)
+  std::vector<int8_t> amsign;      // (-1)^{sum m} of each AA function
   int nprop = 0;
   std::vector<double> ctilde_multi;   // [nprop * nAA]
   void *d_ic_multi = nullptr;         // [nprop * (G+1) * item_n] in the energy type
@@ -115,7 +119,9 @@ namespace ace {
 int kernels_prepare(ace_ctx *ctx);
 int launch_energy_forces(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const double *rr,
                          const int32_t *sp, double *E, double *G, cudaStream_t st,
-                         const void *ic = nullptr, double c0 = 0.0);
+                         const void *ic = nullptr, double c0 = 0.0, bool cpx = false);
+// complex-coefficient (item schedule) energy/force kernels (ace_launch_cplx.cu)
+void *ef_func_cplx(const ace_ctx *ctx, bool grad);
 int launch_basis(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const double *rr,
                  const int32_t *sp, double *B, double *dB, cudaStream_t st);
 int launch_dbasis(ace_ctx *ctx, int64_t nEnv, const int64_t *off_d, const int64_t *off_h, const double *rr,

@@ -203,8 +203,13 @@ template <typename T> __device__ __forceinline__ cpx<T> shfl_down_c(cpx<T> v, in
 
 // ITEMS selects the phase-2 algorithm: false = per-thread trie walk over the
 // lexicographic schedule, true = uniform items (ace_sched.h build_items).
-template <typename TE, typename TG, int K, int NT, bool GRAD, bool ITEMS>
+// CPX (item schedule only): complex coefficients c = (re, im), stored as
+// (G+1) rows of real parts followed by (G+1) rows of imaginary parts; the
+// output is Re(sum_k c_k AA_k) (the Cartesian components of an
+// EuclideanVector model).
+template <typename TE, typename TG, int K, int NT, bool GRAD, bool ITEMS, bool CPX = false>
 __global__ void __launch_bounds__(NT) ef_kernel(EFArgs a) {
+  static_assert(ITEMS || !CPX, "complex coefficients need the item schedule");
   constexpr bool SAME = std::is_same<TE, TG>::value;
   extern __shared__ __align__(16) unsigned char sm[];
   const EFLayout lay = ef_layout(a.ntab, a.nRs, a.L, a.nA, a.chunkE, a.chunkG, a.npriv, NT, sizeof(TE),
@@ -333,7 +338,7 @@ __global__ void __launch_bounds__(NT) ef_kernel(EFArgs a) {
         unsigned heads[IU];
         cpx<TE> bar[IU], H[IU];
         cpx<TG> aG[IU][KP];
-        TE cl[IU][ITEM_G];
+        TE cl[IU][ITEM_G], cli[IU][ITEM_G];
 #pragma unroll
         for (int u = 0; u < IU; ++u) {
           const int64_t f = f0 + (int64_t)u * NT;
@@ -355,12 +360,16 @@ __global__ void __launch_bounds__(NT) ef_kernel(EFArgs a) {
               if (GRAD) aG[u][d] = AG[vi[u][d]];
             }
           }
-          H[u] = {ok ? load_coef<TE>(a.ic, f) : ze, ze};
+          H[u] = {ok ? load_coef<TE>(a.ic, f) : ze, (CPX && ok) ? load_coef<TE>(a.ic, (int64_t)(ITEM_G + 1) * a.in + f) : ze};
 #pragma unroll
           for (int g = 0; g < ITEM_G; ++g) {
             ul[u][g] = (int)((vw[(5 + g) >> 1] >> (16 * ((5 + g) & 1))) & 0xffff);
             cl[u][g] = ok ? load_coef<TE>(a.ic, (int64_t)(g + 1) * a.in + f) : ze;
-            if (g < nl[u]) H[u] = cadd(H[u], cscale(AE[ul[u][g]], cl[u][g]));
+            cli[u][g] = (CPX && ok) ? load_coef<TE>(a.ic, (int64_t)(ITEM_G + 2 + g) * a.in + f) : ze;
+            if (g < nl[u]) {
+              if constexpr (CPX) H[u] = cadd(H[u], cmul(AE[ul[u][g]], cpx<TE>{cl[u][g], cli[u][g]}));
+              else H[u] = cadd(H[u], cscale(AE[ul[u][g]], cl[u][g]));
+            }
           }
         }
 #pragma unroll
@@ -381,7 +390,10 @@ __global__ void __launch_bounds__(NT) ef_kernel(EFArgs a) {
             const cpx<TG> h = {lower<TG>(H[u].re), lower<TG>(H[u].im)};
 #pragma unroll
             for (int g = 0; g < ITEM_G; ++g)
-              if (g < nl[u]) dacc(ul[u][g], cscale(bG, lower<TG>(cl[u][g])));
+              if (g < nl[u]) {
+                if constexpr (CPX) dacc(ul[u][g], cmul(bG, cpx<TG>{lower<TG>(cl[u][g]), lower<TG>(cli[u][g])}));
+                else dacc(ul[u][g], cscale(bG, lower<TG>(cl[u][g])));
+              }
 #pragma unroll
             for (int d = 0; d < KP; ++d)
               v[u][d] = (d < P[u]) ? cmul(cmul(pre[d], suf[d]), h) : cpx<TG>{TG(0), TG(0)};

@@ -129,7 +129,7 @@ int kernels_prepare(ace_ctx *ctx) {
 }
 
 int launch_energy_forces(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const double *rr, const int32_t *sp,
-                         double *E, double *G, cudaStream_t st, const void *ic, double c0) {
+                         double *E, double *G, cudaStream_t st, const void *ic, double c0, bool cpx) {
   if (nEnv == 0) return ACE_OK;
   if (ctx->learned) {
     int rc = learned_radials(ctx, nEnv, off, rr, sp, st);
@@ -138,6 +138,13 @@ int launch_energy_forces(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const d
   EFArgs a = make_args(ctx, nEnv, off, rr, sp, E, G);
   if (ic) { a.ic = ic; a.c0 = c0; }
   void *f = ef_func(ctx, G != nullptr);
+  if (cpx) {
+    f = ef_func_cplx(ctx, G != nullptr);
+    if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ctx->smem) != cudaSuccess) {
+      ctx->err = "cudaFuncSetAttribute failed";
+      return ACE_ERR_CUDA;
+    }
+  }
   const int grid = (int)std::min<int64_t>(nEnv, ctx->grid);
   void *args[] = {&a};
   cudaError_t e = cudaLaunchKernel(f, dim3(grid), dim3(NT), args, ctx->smem, st);

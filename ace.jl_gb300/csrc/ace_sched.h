@@ -38,6 +38,10 @@ struct Schedule {
   std::vector<int32_t> start;      // [nthreads + 1] per-thread ranges
   bool halved = false;
   int64_t nodes = 0;               // trie nodes opened (for accounting)
+  // when halved: the m-reversed partner of every AA function and (-1)^{sum m}
+  // (AA_partner = (-1)^{sum m} conj(AA)), for merging complex coefficients
+  std::vector<int64_t> partner;
+  std::vector<int8_t> msign;
 };
 
 inline Schedule build_schedule(int nA, const int32_t *a_n, const int32_t *a_l, const int32_t *a_m,
@@ -88,6 +92,15 @@ inline Schedule build_schedule(int nA, const int32_t *a_n, const int32_t *a_l, c
     }
   }
   s.halved = ok;
+  if (ok) {
+    s.partner = pk;
+    s.msign.resize(nAA);
+    for (int64_t k = 0; k < nAA; ++k) {
+      int msum = 0;
+      for (int j = 0; j < orders[k]; ++j) msum += a_m[iAA2iA[k * K + j]];
+      s.msign[k] = (msum % 2 == 0) ? 1 : -1;
+    }
+  }
   // ---- kept functions (order >= 1)
   std::vector<int64_t> keep;
   std::vector<uint8_t> wts;

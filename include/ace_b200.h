@@ -121,8 +121,17 @@ int ace_set_ctilde(ace_ctx *ctx, const double *ctilde, int64_t nAA);
 /* Multi-property models (c::Vector{SVector{N}}, src/linearmodel.jl:28-35):
    nprop coefficient sets for one basis, property-major c[p*nB + b]. */
 int ace_set_params_multi(ace_ctx *ctx, const double *c, int64_t nB, int32_t nprop);
+/* Complex AA coefficients for nprop properties, ct[(p*nAA + k)*2 + {0,1}] =
+   (re, im): property p evaluates Re(sum_k ct_pk AA_k).  This is how an
+   EuclideanVector model (src/properties.jl:154-248, B_b = Re(U_b . AA) in
+   R^3 with complex U) is evaluated: one property per Cartesian component
+   with c~^(i) = U_i^T c.  Needs the item schedule; then evaluate with
+   ace_energy_forces_multi. */
+int ace_set_ctilde_complex(ace_ctx *ctx, const double *ct, int64_t nAA, int32_t nprop);
+
 /* Energies E[p*nEnv + e] and gradients dEdrr[(p*nNbr + j)*3 + a] of every
-   property set by ace_set_params_multi (property-major outputs). */
+   property set by ace_set_params_multi or ace_set_ctilde_complex
+   (property-major outputs). */
 int ace_energy_forces_multi(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, const double *rr,
                             const int32_t *species, double *E, double *dEdrr, int32_t flags, void *stream);
 
