@@ -61,13 +61,15 @@ def dist_info():
     return rank, world, local
 
 
-def build_workload(nenv=None):
+def build_workload(nenv=None, rank=0):
+    """The model and this rank's batch: every replica evaluates its own
+    batch of the workload's size (weak scaling), seeded by its rank."""
     from ace_gb300.configs import random_batch
     from ace_gb300.spec import random_coefficients, symmetric_basis
     W = WORKLOAD
     spec = symmetric_basis(W["maxorder"], W["maxdeg"], maxL=W["maxL"], nspecies=W["nspecies"])
     c = random_coefficients(spec, seed=W["seed"])
-    b = random_batch(nenv or W["nenv"], W["jlo"], W["jhi"], nspecies=W["nspecies"], seed=W["seed"],
+    b = random_batch(nenv or W["nenv"], W["jlo"], W["jhi"], nspecies=W["nspecies"], seed=W["seed"] + 7919 * rank,
                      bimodal=W.get("bimodal"))
     return spec, c, b
 
@@ -405,7 +407,7 @@ def main():
         if world > 1:
             dist.barrier()
         return
-    spec, c, b = build_workload(args.nenv)
+    spec, c, b = build_workload(args.nenv, rank)
     nenv, nnbr = b.nenv, b.nnbr
     dev = torch.device("cuda", local)
     off_d = torch.from_numpy(b.offsets).to(dev)
