@@ -96,136 +96,6 @@ __device__ __forceinline__ void radial_eval(const Tables<T> &tb, T r, T *R, T *d
   }
 }
 
-// Complex Y_l^m (index_y order) at direction (x, y, z) (cYlm!), with P scratch
-// of size_p(L).
-template <typename T>
-__device__ __forceinline__ void sh_values(const Tables<T> &tb, T x, T y, T z, T *P, cpx<T> *Y) {
-  const int L = tb.L;
-  const T zero = Arith<T>::zero();
-  const T rho2 = x * x + y * y;
-  const T r = Arith<T>::sqrt_(rho2 + z * z);
-  const T rho = Arith<T>::sqrt_(rho2);
-  const T cost = z / r;
-  const T sint = rho / r;
-  T cosp = Arith<T>::one(), sinp = zero;
-  if (Arith<T>::positive(rho)) { cosp = x / rho; sinp = y / rho; }
-  const T *A = tb.alpA, *B = tb.alpB;
-  T temp = tb.sqhalfpi;
-  P[idx_p(0, 0)] = temp;
-  if (L > 0) {
-    P[idx_p(1, 0)] = cost * tb.sq3 * temp;
-    temp = -tb.sq15 * sint * temp;
-    P[idx_p(1, 1)] = temp;
-    for (int l = 2; l <= L; ++l) {
-      const int il = (l * (l + 1)) / 2, ilm1 = il - l, ilm2 = ilm1 - l + 1;
-      for (int m = 0; m <= l - 2; ++m)
-        P[il + m] = A[il + m] * (cost * P[ilm1 + m] + B[il + m] * P[ilm2 + m]);
-      P[il + l - 1] = cost * tb.alpC[l] * temp;
-      temp = tb.alpD[l] * sint * temp;
-      P[il + l] = temp;
-    }
-  }
-  for (int l = 0; l <= L; ++l) Y[idx_y(l, 0)] = {P[idx_p(l, 0)] * tb.invsqrt2, zero};
-  cpx<T> ep = {tb.invsqrt2, zero};
-  const cpx<T> ef = {cosp, sinp};
-  bool neg = false;
-  for (int m = 1; m <= L; ++m) {
-    neg = !neg;
-    ep = cmul(ep, ef);
-    const cpx<T> em = neg ? cpx<T>{-ep.re, ep.im} : cpx<T>{ep.re, -ep.im};
-    for (int l = m; l <= L; ++l) {
-      const T p = P[idx_p(l, m)];
-      Y[idx_y(l, -m)] = cscale(em, p);
-      Y[idx_y(l, m)] = cscale(ep, p);
-    }
-  }
-}
-
-// Y and its Cartesian gradients dY[3*iy + a] through the cYlm_ed! path.
-template <typename T>
-__device__ __forceinline__ void sh_grad(const Tables<T> &tb, T x, T y, T z, T *P, T *dP,
-                                        cpx<T> *Y, cpx<T> *dY) {
-  const int L = tb.L;
-  const T zero = Arith<T>::zero();
-  const T rho2 = x * x + y * y;
-  const T r = Arith<T>::sqrt_(rho2 + z * z);
-  const T rho = Arith<T>::sqrt_(rho2);
-  const T cost = z / r;
-  const T sint = rho / r;
-  T cosp = Arith<T>::one(), sinp = zero;
-  if (Arith<T>::positive(rho)) { cosp = x / rho; sinp = y / rho; }
-  const T *A = tb.alpA, *B = tb.alpB;
-  T temp = tb.sqhalfpi;
-  P[idx_p(0, 0)] = temp;
-  T temp_d = zero;
-  dP[idx_p(0, 0)] = temp_d;
-  if (L > 0) {
-    P[idx_p(1, 0)] = cost * tb.sq3 * temp;
-    dP[idx_p(1, 0)] = -sint * tb.sq3 * temp + cost * tb.sq3 * temp_d;
-    T temp1 = -tb.sq15 * temp;
-    temp_d = -tb.sq15 * (cost * temp + sint * temp_d);
-    P[idx_p(1, 1)] = temp1;
-    dP[idx_p(1, 1)] = temp_d;
-    const T s2 = sint * sint;
-    for (int l = 2; l <= L; ++l) {
-      P[idx_p(l, 0)] = A[idx_p(l, 0)] * (cost * P[idx_p(l - 1, 0)] + B[idx_p(l, 0)] * P[idx_p(l - 2, 0)]);
-      dP[idx_p(l, 0)] = A[idx_p(l, 0)] * (-sint * P[idx_p(l - 1, 0)] + cost * dP[idx_p(l - 1, 0)] +
-                                          B[idx_p(l, 0)] * dP[idx_p(l - 2, 0)]);
-      for (int m = 1; m <= l - 2; ++m) {
-        P[idx_p(l, m)] = A[idx_p(l, m)] * (cost * P[idx_p(l - 1, m)] + B[idx_p(l, m)] * P[idx_p(l - 2, m)]);
-        dP[idx_p(l, m)] = A[idx_p(l, m)] * (-s2 * P[idx_p(l - 1, m)] + cost * dP[idx_p(l - 1, m)] +
-                                            B[idx_p(l, m)] * dP[idx_p(l - 2, m)]);
-      }
-      const T q = tb.alpC[l];
-      P[idx_p(l, l - 1)] = q * cost * temp1;
-      dP[idx_p(l, l - 1)] = q * (-s2 * temp1 + cost * temp_d);
-      const T f = tb.alpD[l];
-      const T nt1 = f * sint * temp1;
-      const T ntd = f * (cost * temp1 * sint + sint * temp_d);
-      temp1 = nt1;
-      temp_d = ntd;
-      P[idx_p(l, l)] = temp1;
-      dP[idx_p(l, l)] = temp_d;
-    }
-  }
-  const T rinv = Arith<T>::one() / (r + Arith<T>::from(2.220446049250313e-16));
-  const T cc = cosp * cost, sc = sinp * cost;
-  for (int l = 0; l <= L; ++l) {
-    Y[idx_y(l, 0)] = {P[idx_p(l, 0)] * tb.invsqrt2, zero};
-    const T ft = dP[idx_p(l, 0)] * tb.invsqrt2;
-    cpx<T> *d = dY + 3 * idx_y(l, 0);
-    d[0] = {(cc * ft) * rinv, zero};
-    d[1] = {(sc * ft) * rinv, zero};
-    d[2] = {(-(sint * ft)) * rinv, zero};
-  }
-  cpx<T> ep = {tb.invsqrt2 * cosp, tb.invsqrt2 * sinp};
-  const cpx<T> ef = {cosp, sinp};
-  bool neg = false;
-  for (int m = 1; m <= L; ++m) {
-    neg = !neg;
-    if (m > 1) ep = cmul(ep, ef);
-    const cpx<T> em = neg ? cpx<T>{-ep.re, ep.im} : cpx<T>{ep.re, -ep.im};
-    const T fm = Arith<T>::from((double)m);
-    const cpx<T> dep = {-(fm * ep.im), fm * ep.re};
-    const cpx<T> dem = {fm * em.im, -(fm * em.re)};
-    for (int l = m; l <= L; ++l) {
-      const T p = P[idx_p(l, m)];
-      const T dp = dP[idx_p(l, m)];
-      Y[idx_y(l, -m)] = cscale(cscale(em, p), sint);
-      Y[idx_y(l, m)] = cscale(cscale(ep, p), sint);
-#pragma unroll
-      for (int s = 0; s < 2; ++s) {
-        const cpx<T> fps = cscale(s == 0 ? dem : dep, p);
-        const cpx<T> ft = cscale(s == 0 ? em : ep, dp);
-        cpx<T> *d = dY + 3 * idx_y(l, s == 0 ? -m : m);
-        d[0] = {(-(sinp * fps.re) + cc * ft.re) * rinv, (-(sinp * fps.im) + cc * ft.im) * rinv};
-        d[1] = {((cosp * fps.re) + sc * ft.re) * rinv, ((cosp * fps.im) + sc * ft.im) * rinv};
-        d[2] = {(-(sint * ft.re)) * rinv, (-(sint * ft.im)) * rinv};
-      }
-    }
-  }
-}
-
 // ---------------------------------------------------------------------------
 // Column-parallel spherical harmonics: one thread per (neighbour, m), m = 0..L.
 // The associated Legendre recursion of sphericalharmonics.jl:167-267 is a
@@ -233,7 +103,8 @@ __device__ __forceinline__ void sh_grad(const Tables<T> &tb, T x, T y, T z, T *P
 // (itself a short recurrence in m), so each column m is computed in
 // registers by its own thread: seed, P(m+1, m) = sqrt(2m+3) cos(theta) P(m, m),
 // then the three-term recurrence.  Each thread writes Y(l, +-m) (and dY) for
-// l = m..L.  Same formulas and constants as sh_values / sh_grad.
+// l = m..L.  The constants (alpA, alpB, alpC, alpD) are those of the
+// reference's ALP recursion (sphericalharmonics.jl:146-165).
 
 template <typename T> struct Angles { T cost, sint, cosp, sinp, r; };
 
