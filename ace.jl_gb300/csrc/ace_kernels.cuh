@@ -333,6 +333,13 @@ __global__ void __launch_bounds__(NT) ef_kernel(EFArgs a) {
       const int lane = tid & 31;
       const cpx<TG> gone = {TG(1), TG(0)};
       const TE ze = Arith<TE>::zero();
+#if EF_ITEM_RUNS
+      // prefix adjoints of this thread's run: target and running sum per depth
+      int rcur[KP];
+      cpx<TG> racc[KP];
+#pragma unroll
+      for (int d = 0; d < KP; ++d) { rcur[d] = -1; racc[d] = {TG(0), TG(0)}; }
+#endif
       for (int64_t f0 = tid; f0 < a.in; f0 += (int64_t)IU * NT) {
         int P[IU], nl[IU], vi[IU][KP], ul[IU][ITEM_G];
         unsigned heads[IU];
@@ -398,6 +405,23 @@ __global__ void __launch_bounds__(NT) ef_kernel(EFArgs a) {
             for (int d = 0; d < KP; ++d)
               v[u][d] = (d < P[u]) ? cmul(cmul(pre[d], suf[d]), h) : cpx<TG>{TG(0), TG(0)};
           }
+#if EF_ITEM_RUNS
+#pragma unroll
+          for (int u = 0; u < IU; ++u)
+#pragma unroll
+            for (int d = 0; d < KP; ++d) {
+              if (d < P[u]) {
+                if (vi[u][d] != rcur[d]) {
+                  if (rcur[d] >= 0) dacc(rcur[d], racc[d]);
+                  rcur[d] = vi[u][d];
+                  racc[d] = v[u][d];
+                } else {
+                  racc[d].re += v[u][d].re;
+                  racc[d].im += v[u][d].im;
+                }
+              }
+            }
+#else
 #pragma unroll
           for (int d = 0; d < KP; ++d) {
             if (d < KP - 1) {
@@ -424,8 +448,16 @@ __global__ void __launch_bounds__(NT) ef_kernel(EFArgs a) {
                 if (d < P[u]) dacc(vi[u][d], v[u][d]);
             }
           }
+#endif
         }
       }
+#if EF_ITEM_RUNS
+      if (GRAD) {
+#pragma unroll
+        for (int d = 0; d < KP; ++d)
+          if (rcur[d] >= 0) dacc(rcur[d], racc[d]);
+      }
+#endif
     }
     const double esum = block_sum(lower<double>(eacc), red);
     if (tid == 0) a.E[e] = a.c0 + esum;

@@ -193,6 +193,14 @@ inline Interleaved interleave(const Schedule &s, int nthreads) {
 // P | nleaf << 4, byte 15 = head bits.  P == 0 marks padding.
 static constexpr int ITEM_G = 2;
 
+// item layout: 1 (default) = per-thread contiguous runs with
+// register-accumulated prefix adjoints (measured on GB300: FP64 +13-26 %,
+// fp32x2 unchanged); 0 = uniform stride with warp-segmented prefix
+// reductions using the head bits
+#ifndef EF_ITEM_RUNS
+#define EF_ITEM_RUNS 1
+#endif
+
 struct ItemSchedule {
   int K = 0, KP = 0;               // max order, max prefix length (K - 1)
   int64_t n = 0;                   // items, padded to a multiple of the block size
@@ -236,13 +244,28 @@ inline ItemSchedule build_items(const Schedule &s, int nthreads) {
   const int64_t n0 = (int64_t)items.size();
   it.n = ((n0 + nthreads - 1) / nthreads) * nthreads;
   if (it.n == 0) it.n = nthreads;
+#if EF_ITEM_RUNS
+  // each thread takes a contiguous run of the sorted items, interleaved
+  // (slot = j * nthreads + thread): consecutive items of a thread share
+  // prefixes, so the kernel keeps their prefix adjoints in registers
+  {
+    const int64_t R = it.n / nthreads;
+    std::vector<Item> laid(it.n);
+    for (int64_t i = 0; i < n0; ++i) laid[(i % R) * nthreads + i / R] = items[i];
+    items.swap(laid);
+  }
+  const int64_t nfill = it.n;
+#else
+  const int64_t nfill = n0;
+#endif
   it.rec.assign((size_t)it.n * 8, 0);
   it.kown.assign(it.n, -1);
   it.kleaf.assign((size_t)it.n * ITEM_G, -1);
   it.wown.assign(it.n, 0);
   it.wleaf.assign((size_t)it.n * ITEM_G, 0);
-  for (int64_t f = 0; f < n0; ++f) {
+  for (int64_t f = 0; f < nfill; ++f) {
     const Item &x = items[f];
+    if (x.pre.empty() && x.leaves.empty() && x.kown < 0) continue;  // padding
     uint16_t *r = &it.rec[8 * f];
     const int P = (int)x.pre.size();
     for (int d = 0; d < P; ++d) r[d] = (uint16_t)x.pre[d];
@@ -268,7 +291,9 @@ inline ItemSchedule build_items(const Schedule &s, int nthreads) {
     b[14] = (uint8_t)(P | (nl << 4));
     b[15] = heads;
   }
+#if !EF_ITEM_RUNS
   for (int64_t f = n0; f < it.n; ++f) ((uint8_t *)&it.rec[8 * f])[15] = 0x1f;  // padding: own segments
+#endif
   return it;
 }
 

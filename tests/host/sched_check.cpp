@@ -77,11 +77,49 @@ int main(int argc, char **argv) {
     for (int e = K; e >= 1; --e) if (e <= cur) close(e);
     Et += H[0].real();
   }
-  // (2) items, 32 consecutive items per warp, segmented by head bits
+  // (2) items
   ItemSchedule it = build_items(s, NT);
   double Ei = ct[0];
   std::vector<C> Di(nA);
   const int KP = it.KP, G = ITEM_G;
+#if EF_ITEM_RUNS
+  // per-thread contiguous runs (slot = j * NT + thread), prefix adjoints
+  // accumulated per depth and flushed when the target changes, as the kernel
+  for (int t = 0; t < NT; ++t) {
+    int cur[8];
+    C acc[8];
+    for (int e = 0; e < 8; ++e) { cur[e] = -1; acc[e] = 0; }
+    for (int64_t f = t; f < it.n; f += NT) {
+      const uint16_t *r = &it.rec[8 * f];
+      const uint8_t *b = (const uint8_t *)r;
+      const int P = b[14] & 0xf, nl = b[14] >> 4;
+      auto coef = [&](int g) {
+        int64_t k = g == 0 ? it.kown[f] : it.kleaf[f * G + g - 1];
+        uint8_t w = g == 0 ? it.wown[f] : it.wleaf[f * G + g - 1];
+        return k < 0 ? 0.0 : w * ct[k];
+      };
+      C bar = 1;
+      for (int e = 0; e < P; ++e) bar *= A[r[e]];
+      C H = coef(0);
+      for (int g = 0; g < nl; ++g) H += coef(g + 1) * A[r[5 + g]];
+      if (P > 0) Ei += (bar * H).real();
+      for (int g = 0; g < nl; ++g) Di[r[5 + g]] += coef(g + 1) * bar;
+      for (int e = 0; e < P; ++e) {
+        C q = H;
+        for (int x = 0; x < P; ++x) if (x != e) q *= A[r[x]];
+        if (r[e] != cur[e]) {
+          if (cur[e] >= 0) Di[cur[e]] += acc[e];
+          cur[e] = r[e];
+          acc[e] = q;
+        } else {
+          acc[e] += q;
+        }
+      }
+    }
+    for (int e = 0; e < KP; ++e) if (cur[e] >= 0) Di[cur[e]] += acc[e];
+  }
+#else
+  // 32 consecutive items per warp, segmented by head bits
   for (int64_t w0 = 0; w0 < it.n; w0 += 32) {
     C v[32][8];
     int tgt[32][8];
@@ -124,6 +162,7 @@ int main(int argc, char **argv) {
       }
     }
   }
+#endif
   // the kernels' adjoint is exact along conjugation-symmetric directions W
   C gr = 0, gt = 0, gi = 0;
   for (int i = 0; i < nA; ++i) { gr += Dref[i] * W[i]; gt += Dt[i] * W[i]; gi += Di[i] * W[i]; }
