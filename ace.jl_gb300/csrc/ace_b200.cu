@@ -245,16 +245,16 @@ extern "C" int ace_ctx_create(const ace_spec_bundle *s, int32_t prec, int32_t de
       g_create_error = ctx->err;
       return fail(rc);
     }
-    // fused basis table for the FP32-based forms (measured faster there); the
-    // FP64 form keeps the AA-scratch path, whose flat products are fewer
-    // (nAA instead of nnz(U)).  ACE_B200_BASIS=fused|materialised overrides.
+    // fused basis table (measured faster than the AA-scratch path in every
+    // form); ACE_B200_BASIS=materialised keeps the AA-scratch path
     const char *benv = getenv("ACE_B200_BASIS");
-    ctx->fused_basis = (prec != ACE_PREC_FP64);
+    ctx->fused_basis = true;
     if (benv && std::string(benv) == "materialised") ctx->fused_basis = false;
     if (benv && std::string(benv) == "fused") ctx->fused_basis = true;
-    if (s->nB >= (int64_t(1) << 27)) ctx->fused_basis = false;
+    if (s->nB >= (int64_t(1) << 24)) ctx->fused_basis = false;
     if (ctx->fused_basis) {
-      URows ur = build_urows(s->nB, s->U_indptr, s->U_indices, s->U_data, s->orders, s->iAA2iA, s->maxord, 128);
+      URows ur = build_urows(s->nB, s->U_indptr, s->U_indices, s->U_data, s->orders, s->iAA2iA, s->maxord, 128,
+                             ctx->apartner);
       ctx->ulen = ur.len;
       const size_t csz = (prec == ACE_PREC_FP32 || prec == ACE_PREC_FP32_BF16X3) ? 4 : 8;
       if ((rc = upload(ctx, (uint32_t **)&ctx->d_urec, ur.rec.data(), ur.rec.size()))) {

@@ -614,10 +614,11 @@ __global__ void ub_kernel(int64_t ne, int64_t e0, int64_t ldE, int64_t nB, const
 }
 
 // Fused B = U real(AA) per environment, without AA in memory: phase 1 (A in
-// shared memory), then each thread walks its U rows' entries (ace_sched.h
-// build_urows), forms real(AA_k) = Re(prod A) (src/pibasis.jl:265-275) and
-// accumulates U[b, k] real(AA_k); a row's sum is written at its last entry
-// (genmul!, src/symmbasis.jl:248-264).
+// shared memory), then each thread walks its entries (ace_sched.h
+// build_urows): one AA function per entry, real(AA_k) = Re(prod A)
+// (src/pibasis.jl:265-275) formed once and added with the entry's U values
+// to the row accumulators of its group; a group's rows are written at its
+// last entry (genmul!, src/symmbasis.jl:248-264).
 template <typename TE>
 __global__ void __launch_bounds__(128) ub_fused_kernel(EFArgs a, const uint4 *urec, const void *uval, int64_t ulen,
                                                        int64_t nB, double *B) {
@@ -644,13 +645,15 @@ __global__ void __launch_bounds__(128) ub_fused_kernel(EFArgs a, const uint4 *ur
       continue;
     }
     build_A<TE>(a, tb, o0, (int)(o1 - o0), a.chunkE, lay.slabE, s_an, s_aiy, s_amu, ssp, (TE *)(sm + lay.slab), AE);
-    TE acc = ze;
+    TE acc[UB_R];
+#pragma unroll
+    for (int i = 0; i < UB_R; ++i) acc[i] = ze;
     double *Be = B + e * nB;
     for (int64_t j = 0; j < ulen; ++j) {
       const int64_t slot = j * nt + tid;
       const uint4 rc = urec[slot];
       if (!(rc.w >> 31)) break;  // padding only follows a thread's last entry
-      const int ord = (rc.w >> 27) & 7;
+      const int ord = (rc.w >> 24) & 7;
       const uint32_t vw[3] = {rc.x, rc.y, rc.z};
       cpx<TE> p = {Arith<TE>::one(), ze};
 #pragma unroll
@@ -660,10 +663,16 @@ __global__ void __launch_bounds__(128) ub_fused_kernel(EFArgs a, const uint4 *ur
           p = (t == 0) ? av : cmul(p, av);
         }
       }
-      acc = acc + load_coef<TE>(uval, slot) * p.re;
+#pragma unroll
+      for (int i = 0; i < UB_R; ++i) acc[i] = acc[i] + load_coef<TE>(uval, slot * UB_R + i) * p.re;
       if ((rc.w >> 30) & 1u) {
-        Be[rc.w & ((1u << 27) - 1u)] = lower<double>(acc);
-        acc = ze;
+        const int r = (int)((rc.w >> 27) & 7u) + 1;
+        const int64_t b0 = rc.w & ((1u << 24) - 1u);
+#pragma unroll
+        for (int i = 0; i < UB_R; ++i) {
+          if (i < r) Be[b0 + i] = lower<double>(acc[i]);
+          acc[i] = ze;
+        }
       }
     }
     __syncthreads();

@@ -297,60 +297,104 @@ inline ItemSchedule build_items(const Schedule &s, int nthreads) {
   return it;
 }
 
-// Fused symmetric-basis table (B = U real(AA) without AA in memory): the
-// nonzeros of U in row order, rows assigned to threads longest first, each to
-// the least-loaded thread, and each thread's entries interleaved
-// (slot = j * nthreads + thread) so a warp's loads are contiguous.  Record
-// (16 bytes): x, y, z = the AA function's A indices v0..v5 (uint16 pairs),
-// w = row | ord << 27 | last-of-row << 30 | valid << 31.  A row without
-// nonzeros gets one entry of value 0 so that its B value is written.
+// Fused symmetric-basis table (B = U real(AA) without AA in memory).  U's
+// rows are grouped into classes -- consecutive rows whose AA columns overlap
+// (the rows of one (n, l)-class; different classes use disjoint AA
+// functions) -- of at most UB_R rows.  Each AA function of a group is one
+// entry: the kernel forms real(AA_k) once and adds U[b, k] real(AA_k) to the
+// group's UB_R row accumulators.  With a halved schedule an AA function and
+// its m-reversed partner (equal real parts for invariants) share one entry
+// whose values are the sum of both U columns.  Groups are assigned to
+// threads longest first, each to the least-loaded thread, and each thread's
+// entries interleaved (slot = j * nthreads + thread).
+// Record (16 bytes): x, y, z = A indices v0..v5 (uint16 pairs),
+// w = b0 | ord << 24 | (r - 1) << 27 | last-of-group << 30 | valid << 31
+// (b0 = the group's first row, r = its rows); values [slot][UB_R].
+static constexpr int UB_R = 8;
+
 struct URows {
   int64_t len = 0;                 // slots per thread
   std::vector<uint32_t> rec;       // [len * nthreads * 4]
-  std::vector<double> val;         // [len * nthreads]
+  std::vector<double> val;         // [len * nthreads * UB_R]
 };
 
 inline URows build_urows(int64_t nB, const int64_t *Uptr, const int32_t *Uidx, const double *Uval,
-                         const int32_t *orders, const int32_t *iAA2iA, int K, int nthreads) {
-  URows u;
-  std::vector<int64_t> rows(nB);
-  for (int64_t b = 0; b < nB; ++b) rows[b] = b;
-  auto rlen = [&](int64_t b) { return std::max<int64_t>(1, Uptr[b + 1] - Uptr[b]); };
-  std::stable_sort(rows.begin(), rows.end(), [&](int64_t x, int64_t y) { return rlen(x) > rlen(y); });
-  std::vector<std::vector<int64_t>> own(nthreads);
-  std::vector<int64_t> load(nthreads, 0);
+                         const int32_t *orders, const int32_t *iAA2iA, int K, int nthreads,
+                         const std::vector<int64_t> &partner) {
+  struct Group { int64_t b0 = 0; int r = 0; std::vector<int64_t> cols; std::vector<double> vals; };
+  std::vector<Group> groups;
+  // row grouping
+  {
+    int64_t b = 0;
+    while (b < nB) {
+      Group g;
+      g.b0 = b;
+      std::vector<int64_t> cols(Uidx + Uptr[b], Uidx + Uptr[b + 1]);
+      int r = 1;
+      while (b + r < nB && r < UB_R) {
+        bool overlap = false;
+        for (int64_t q = Uptr[b + r]; q < Uptr[b + r + 1] && !overlap; ++q)
+          overlap = std::find(cols.begin(), cols.end(), (int64_t)Uidx[q]) != cols.end();
+        if (!overlap) break;
+        cols.insert(cols.end(), Uidx + Uptr[b + r], Uidx + Uptr[b + r + 1]);
+        ++r;
+      }
+      g.r = r;
+      // representative columns (a partner pair maps to its smaller index)
+      auto rep = [&](int64_t k) { return partner.empty() ? k : std::min(k, partner[k]); };
+      std::vector<int64_t> reps;
+      for (int64_t k : cols) reps.push_back(rep(k));
+      std::sort(reps.begin(), reps.end());
+      reps.erase(std::unique(reps.begin(), reps.end()), reps.end());
+      g.cols = reps;
+      g.vals.assign(reps.size() * UB_R, 0.0);
+      for (int i = 0; i < r; ++i)
+        for (int64_t q = Uptr[b + i]; q < Uptr[b + i + 1]; ++q) {
+          const int64_t c = std::lower_bound(reps.begin(), reps.end(), rep(Uidx[q])) - reps.begin();
+          g.vals[c * UB_R + i] += Uval[q];
+        }
+      if (g.cols.empty()) { g.cols.push_back(-1); g.vals.assign(UB_R, 0.0); }  // rows without nonzeros
+      groups.push_back(std::move(g));
+      b += r;
+    }
+  }
+  // assignment to threads
+  std::vector<size_t> order(groups.size());
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) { return groups[x].cols.size() > groups[y].cols.size(); });
+  std::vector<std::vector<size_t>> own(nthreads);
   using P = std::pair<int64_t, int>;
   std::priority_queue<P, std::vector<P>, std::greater<P>> pq;
   for (int t = 0; t < nthreads; ++t) pq.push({0, t});
-  for (int64_t b : rows) {
+  URows u;
+  for (size_t gi : order) {
     P top = pq.top();
     pq.pop();
-    own[top.second].push_back(b);
-    top.first += rlen(b);
-    load[top.second] = top.first;
+    own[top.second].push_back(gi);
+    top.first += (int64_t)groups[gi].cols.size();
+    u.len = std::max(u.len, top.first);
     pq.push(top);
   }
-  for (int t = 0; t < nthreads; ++t) u.len = std::max(u.len, load[t]);
   u.rec.assign((size_t)u.len * nthreads * 4, 0u);
-  u.val.assign((size_t)u.len * nthreads, 0.0);
+  u.val.assign((size_t)u.len * nthreads * UB_R, 0.0);
   for (int t = 0; t < nthreads; ++t) {
     int64_t j = 0;
-    for (int64_t b : own[t]) {
-      const int64_t k0 = Uptr[b], k1 = Uptr[b + 1];
-      for (int64_t q = k0; q < std::max(k1, k0 + 1); ++q, ++j) {
+    for (size_t gi : own[t]) {
+      const Group &g = groups[gi];
+      for (size_t c = 0; c < g.cols.size(); ++c, ++j) {
         const size_t slot = (size_t)j * nthreads + t;
         uint32_t *r = &u.rec[4 * slot];
-        const bool empty = (k1 == k0);
-        const int64_t k = empty ? -1 : Uidx[q];
-        const int ord = empty ? 0 : orders[k];
+        const int64_t k = g.cols[c];
+        const int ord = k < 0 ? 0 : orders[k];
         uint16_t v[6] = {0, 0, 0, 0, 0, 0};
         for (int d = 0; d < ord; ++d) v[d] = (uint16_t)iAA2iA[k * K + d];
         r[0] = v[0] | ((uint32_t)v[1] << 16);
         r[1] = v[2] | ((uint32_t)v[3] << 16);
         r[2] = v[4] | ((uint32_t)v[5] << 16);
-        const bool last = (q + 1 >= std::max(k1, k0 + 1));
-        r[3] = (uint32_t)b | ((uint32_t)ord << 27) | ((last ? 1u : 0u) << 30) | (1u << 31);
-        u.val[slot] = empty ? 0.0 : Uval[q];
+        const bool last = (c + 1 == g.cols.size());
+        r[3] = (uint32_t)g.b0 | ((uint32_t)ord << 24) | ((uint32_t)(g.r - 1) << 27) | ((last ? 1u : 0u) << 30) |
+               (1u << 31);
+        for (int i = 0; i < UB_R; ++i) u.val[slot * UB_R + i] = g.vals[c * UB_R + i];
       }
     }
   }
