@@ -40,6 +40,13 @@ __host__ __device__ inline size_t al16(size_t x) { return (x + 15) & ~size_t(15)
 #ifndef EF_ITEM_ILP
 #define EF_ITEM_ILP 2
 #endif
+// minimum resident CTAs per SM requested from the register allocator (0:
+// no request).  Measured on GB300 with the fp32x2 form: 6 gives +11 % on
+// order 5 / degree 16 but -3 % on order 4 / degree 12; an explicit 1 lets the
+// allocator take 150-210 registers and costs a third of the throughput.
+#ifndef EF_MIN_BLOCKS
+#define EF_MIN_BLOCKS 0
+#endif
 
 struct EFArgs {
   int64_t nEnv;
@@ -208,7 +215,11 @@ template <typename T> __device__ __forceinline__ cpx<T> shfl_down_c(cpx<T> v, in
 // output is Re(sum_k c_k AA_k) (the Cartesian components of an
 // EuclideanVector model).
 template <typename TE, typename TG, int K, int NT, bool GRAD, bool ITEMS, bool CPX = false>
+#if EF_MIN_BLOCKS > 0
+__global__ void __launch_bounds__(NT, EF_MIN_BLOCKS) ef_kernel(EFArgs a) {
+#else
 __global__ void __launch_bounds__(NT) ef_kernel(EFArgs a) {
+#endif
   static_assert(ITEMS || !CPX, "complex coefficients need the item schedule");
   constexpr bool SAME = std::is_same<TE, TG>::value;
   extern __shared__ __align__(16) unsigned char sm[];
