@@ -677,13 +677,18 @@ __global__ void __launch_bounds__(128) ub_fused_kernel(EFArgs a, const uint4 *ur
 #pragma unroll
       for (int i = 0; i < UB_R; ++i) acc[i] = acc[i] + load_coef<TE>(uval, slot * UB_R + i) * p.re;
       if ((rc.w >> 30) & 1u) {
+        // write the group's r rows; the accumulators shift down so that only
+        // r conversions to double (FP64-pipe work on GB300) are issued
         const int r = (int)((rc.w >> 27) & 7u) + 1;
-        const int64_t b0 = rc.w & ((1u << 24) - 1u);
+        double *Bo = Be + (rc.w & ((1u << 24) - 1u));
+        for (int i = 0; i < r; ++i) {
+          Bo[i] = lower<double>(acc[0]);
 #pragma unroll
-        for (int i = 0; i < UB_R; ++i) {
-          if (i < r) Be[b0 + i] = lower<double>(acc[i]);
-          acc[i] = ze;
+          for (int q = 0; q < UB_R - 1; ++q) acc[q] = acc[q + 1];
+          acc[UB_R - 1] = ze;
         }
+#pragma unroll
+        for (int i = 0; i < UB_R; ++i) acc[i] = ze;
       }
     }
     __syncthreads();

@@ -555,7 +555,7 @@ def main():
         traffic = tr["dram_bytes_per_env"] * nenv
     roof = {"bound": "fp32", "achieved": achieved, "peak": peaks["fp32_tflops"], "unit": "TFLOP/s",
             "frac": achieved / peaks["fp32_tflops"], "traffic": traffic,
-            "kernel": "ef_kernel<df, float> (fused 1p basis, A, AA trie energy + adjoint, forces)",
+            "kernel": "ef_kernel<df, float> (fused 1p basis, A, item-schedule AA energy + adjoint, forces)",
             "peak_source": "measured in this run: cuBLAS SGEMM 8192^3, TF32 off (CUDA-core FP32)",
             "flops_per_env": fl / nenv}
     cpu = None if args.no_cpu else cpu_baseline(spec, c, b)
