@@ -74,6 +74,11 @@ def build_workload(nenv=None, rank=0):
     return spec, c, b
 
 
+def _ptr_dev(t):
+    import ctypes
+    return None if t is None else ctypes.c_void_p(int(t.data_ptr()))
+
+
 def flops_per_env(spec, J):
     """Algorithmic FLOPs of one environment with J neighbours, counted on the
     reference algorithm (src/evaluator.jl:121-200) with complex*complex = 6,
@@ -477,6 +482,26 @@ def main():
     value = nenv * args.steps * world / t32
     ms = 1e3 * t32 / args.steps
 
+    # energies only (evaluate without grad_config), chosen form
+    E_only = {}
+    for _ in range(max(1, args.warmup)):
+        ctx.lib.ace_energy(ctx.h, nenv, _ptr_dev(off_d), _ptr_dev(rr_d), _ptr_dev(sp_d), _ptr_dev(E_d), 3 | 4,
+                           stream.cuda_stream)
+    torch.cuda.synchronize()
+    te = 0.0
+    ke = max(1, min(args.steps, 5))
+    for _ in range(ke):
+        flush.zero_()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        ctx.lib.ace_energy(ctx.h, nenv, _ptr_dev(off_d), _ptr_dev(rr_d), _ptr_dev(sp_d), _ptr_dev(E_d), 3 | 4,
+                           stream.cuda_stream)
+        e.record(stream)
+        e.synchronize()
+        te += s.elapsed_time(e) / 1e3
+    ctx.sync()
+    E_only["fp32x2_energy_only"] = {"value": nenv * ke / te, "ms_per_step": 1e3 * te / ke}
+
     # the symmetric basis B = U real(AA) (grad_params, the design matrix), FP64
     # and fp32x2, on a prefix of the batch with B within 4 GB
     nbe = int(min(nenv, max(1, (4 << 30) // (8 * spec.nB))))
@@ -569,7 +594,7 @@ def main():
             "forms": {"fp64": {"value": n64 * k64 * world / t64, "ms_per_step": 1e3 * t64 / k64, "envs": n64},
                       "fp32": {"value": nenv * args.steps * world / t32p, "ms_per_step": 1e3 * t32p / args.steps,
                                "error": err32},
-                      "fp32x2": {"value": value, "ms_per_step": ms, "error": err}, **basis},
+                      "fp32x2": {"value": value, "ms_per_step": ms, "error": err}, **E_only, **basis},
             "error": err, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
             "gpu_launches": int(launches), "peaks_measured": peaks}
     print(json.dumps(line), flush=True)
