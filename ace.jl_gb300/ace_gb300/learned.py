@@ -26,8 +26,8 @@ the teacher by distillation:
 
 ``LearnedRadialModel`` evaluates the student and sends every environment
 with a neighbour outside the training radii (or a species the MLP was not
-trained on) to the teacher, the plain model, which is also the judge of the
-student's error.
+trained on) to the teacher, the plain model, against which the student's
+error is also measured.
 
 Training runs on the GPU through the library's kernels; torch only holds the
 device buffers and forms the elementwise loss residuals.
