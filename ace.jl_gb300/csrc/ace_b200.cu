@@ -410,7 +410,6 @@ extern "C" int ace_set_ctilde_complex(ace_ctx *ctx, const double *ct, int64_t nA
   if (!ctx || !ct) return ctx_fail(ctx, ACE_ERR_INVALID, "NULL argument");
   if (nAA != ctx->nAA) return ctx_fail(ctx, ACE_ERR_INVALID, "length of ctilde != nAA");
   if (nprop < 1 || nprop > 4096) return ctx_fail(ctx, ACE_ERR_INVALID, "nprop out of range [1, 4096]");
-  if (!ctx->use_items) return ctx_fail(ctx, ACE_ERR_UNSUPPORTED, "complex coefficients need the item schedule");
   ACE_CUDA(cudaSetDevice(ctx->device));
   const size_t csz = (ctx->prec == ACE_PREC_FP64 || ctx->prec == ACE_PREC_FP32X2) ? 8 : 4;
   const int64_t ns = (int64_t)ctx->ik.size();
@@ -701,7 +700,10 @@ extern "C" int ace_energy_forces_multi(ace_ctx *ctx, int64_t nEnv, const int64_t
   const int np = ctx->nprop;
   const size_t csz = (ctx->prec == ACE_PREC_FP64 || ctx->prec == ACE_PREC_FP32X2) ? 8 : 4;
   const size_t per = (ctx->cplx ? 2 : 1) * ctx->ik.size() * csz;
-  if (!ctx->use_items) return ctx_fail(ctx, ACE_ERR_UNSUPPORTED, "multi-property models need the item schedule");
+  // real coefficient sets follow the context's schedule choice; complex ones
+  // always run the item kernels
+  if (!ctx->use_items && !ctx->cplx)
+    return ctx_fail(ctx, ACE_ERR_UNSUPPORTED, "multi-property models need the item schedule");
   std::vector<std::pair<void *, size_t>> outs = {{E, (size_t)np * nEnv * sizeof(double)},
                                                  {dEdrr, (size_t)np * nNbr * 3 * sizeof(double)}};
   return drive(ctx, nEnv, offsets, rr, species, flags, stream, outs,

@@ -417,3 +417,26 @@ def test_host_pipeline(lib, oracle_mod):
     # the context stays usable
     E2, _ = ctx.energy_forces(b.offsets, b.rr)
     assert np.array_equal(E2, E)
+
+
+def test_host_pipeline_species(lib):
+    """The host pipeline with a multi-species spec and species arrays."""
+    torch = pytest.importorskip("torch")
+    spec = symmetric_basis(3, 6, maxL=6, nspecies=3)
+    c = random_coefficients(spec, seed=7)
+    ctx = lib.Context(spec, "fp32x2")
+    ctx.set_params(c)
+    b = random_batch(12000, 4, 16, nspecies=3, seed=19)
+    E, G = ctx.energy_forces(b.offsets, b.rr, b.species)
+    dev = torch.device("cuda", 0)
+    Ed = torch.empty(b.nenv, dtype=torch.float64, device=dev)
+    Gd = torch.empty((b.nnbr, 3), dtype=torch.float64, device=dev)
+    ctx.energy_forces_device(torch.from_numpy(b.offsets).to(dev), torch.from_numpy(b.rr).to(dev),
+                             torch.from_numpy(b.species).to(dev), Ed, Gd)
+    assert np.array_equal(E, Ed.cpu().numpy())
+    # FP32 adjoint accumulated with shared-memory atomics: order-dependent rounding
+    assert relerr(G, Gd.cpu().numpy()) <= 1e-6
+    bad = b.species.copy()
+    bad[b.offsets[11000]] = 5
+    with pytest.raises(lib.AceError):
+        ctx.energy_forces(b.offsets, b.rr, bad)

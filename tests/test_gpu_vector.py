@@ -77,3 +77,16 @@ def test_vector_model_covariance_and_gradient(lib, vmodel_inputs):
                 xm = x.copy(); xm[j, a] -= h
                 fd = (model.evaluate(xp) - model.evaluate(xm)) / (2 * h)
                 assert np.allclose(G[e][j, :, a], fd, rtol=1e-6, atol=1e-7 * np.max(np.abs(V)))
+
+
+def test_vector_model_after_autotune_to_trie(lib, vmodel_inputs, monkeypatch):
+    """Complex coefficients run the item kernels whatever schedule the
+    context's real-coefficient calls use."""
+    monkeypatch.setenv("ACE_B200_KERNEL", "trie")
+    spec, c = vmodel_inputs
+    model = LinearVectorModel(spec, c, precision="fp64")
+    monkeypatch.delenv("ACE_B200_KERNEL")
+    ref = LinearVectorModel(spec, c, precision="fp64")
+    b = random_batch(20, 8, 16, seed=2)
+    cfgs = [b.rr[b.offsets[e]:b.offsets[e + 1]] for e in range(b.nenv)]
+    assert np.allclose(model.evaluate(cfgs), ref.evaluate(cfgs), rtol=1e-12, atol=1e-14)
