@@ -135,24 +135,66 @@ class _Trainer:
         return self.mlp.params
 
 
+def pca_radial_targets(teacher: ACESpec, K: int, L: int, r: np.ndarray, sp: np.ndarray, chunk: int = 200_000):
+    """Species-aware radial targets: for every l, the K leading principal
+    directions (over the samples) of the teacher's radial x species channels
+    R_n(r) [s = s'] with (n-1) + l <= maxdeg -- the best K-dimensional linear
+    compression of the channels the teacher's A entries of that l use -- each
+    scaled to unit RMS.  Returns (N, K (L+1)) float32, channel k + K l."""
+    S = teacher.nspecies
+    deg = float(teacher.info.get("maxdeg", len(teacher.radial.J.A)))
+    nR = len(teacher.radial.J.A)
+    N = len(r)
+    out = np.zeros((N, K * (L + 1)), dtype=np.float32)
+    for l in range(L + 1):
+        nl = int(min(nR, np.floor(deg - l + 1e-9) + 1))
+        if nl <= 0:
+            continue
+        G = np.zeros((nl * S, nl * S))
+        for i0 in range(0, N, chunk):
+            R = teacher.radial.evaluate(r[i0:i0 + chunk])[:, :nl]
+            X = np.zeros((len(R), nl * S))
+            for s_ in range(S):
+                m = sp[i0:i0 + chunk] == s_
+                X[m, s_ * nl:(s_ + 1) * nl] = R[m]
+            G += X.T @ X
+        w, V = np.linalg.eigh(G / N)
+        V = V[:, ::-1][:, :K]
+        w = np.maximum(w[::-1][:K], 1e-30)
+        kk = V.shape[1]
+        for i0 in range(0, N, chunk):
+            R = teacher.radial.evaluate(r[i0:i0 + chunk])[:, :nl]
+            X = np.zeros((len(R), nl * S))
+            for s_ in range(S):
+                m = sp[i0:i0 + chunk] == s_
+                X[m, s_ * nl:(s_ + 1) * nl] = R[m]
+            out[i0:i0 + chunk, K * l:K * l + kk] = (X @ V) / np.sqrt(w)
+    return out
+
+
 def pretrain_radial(ctx: Context, mlp: RadialMLP, spec: ACESpec, nsamples: int = 2_000_000, steps: int = 1500,
                     batch: int = 32768, lr: float = 2e-3, rlo: float = 0.8, rhi: float = 5.0, seed: int = 7,
-                    log=None):
-    """Regress the MLP's channels (k, l) onto the student spec's polynomial
-    R_k(r) for every l and species, on seeded neighbour samples r ~ U[rlo,
-    rhi], species uniform; returns the loss history."""
+                    teacher: ACESpec | None = None, log=None):
+    """Regress the MLP's channels (k, l) on seeded neighbour samples r ~
+    U[rlo, rhi], species uniform, onto either the teacher's compressed
+    radial x species channels (``pca_radial_targets``, when a teacher spec is
+    given) or the student spec's own polynomial R_k(r) for every l and
+    species (the species-blind radial basis of width K); returns the loss
+    history."""
     torch = _torch()
     dev = torch.device("cuda", ctx.device)
     rng = np.random.default_rng(seed)
     r = rlo + (rhi - rlo) * rng.random(nsamples)
     sp = rng.integers(0, mlp.nspecies, nsamples).astype(np.int32)
-    Rk = spec.radial.evaluate(r)[:, :mlp.K]                      # (n, K)
     rr = np.zeros((nsamples, 3))
     rr[:, 0] = r
     rr_d = torch.from_numpy(rr).to(dev)
     sp_d = torch.from_numpy(sp).to(dev)
-    T_d = torch.from_numpy(Rk.astype(np.float32)).to(dev)
     C = mlp.C
+    if teacher is not None:
+        T_d = torch.from_numpy(pca_radial_targets(teacher, mlp.K, mlp.L, r, sp)).to(dev)
+    else:
+        T_d = torch.from_numpy(spec.radial.evaluate(r)[:, :mlp.K].astype(np.float32)).to(dev)
     out = torch.empty((batch, 2 * C), dtype=torch.float32, device=dev)
     tr = _Trainer(ctx, mlp, dev)
     hist = []
@@ -167,7 +209,7 @@ def pretrain_radial(ctx: Context, mlp: RadialMLP, spec: ACESpec, nsamples: int =
         rb, sb = rr_d[idx].contiguous(), sp_d[idx].contiguous()
         ctx.radial_mlp_forward(rb, sb, out)
         R = out[:, :C]
-        T = T_d[idx].repeat(1, mlp.L + 1)
+        T = T_d[idx] if teacher is not None else T_d[idx].repeat(1, mlp.L + 1)
         diff = R - T
         gR = (2.0 / (batch * C)) * diff
         tr.g.zero_()

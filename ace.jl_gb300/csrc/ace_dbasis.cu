@@ -218,7 +218,7 @@ static int run_daa(ace_ctx *ctx, int64_t nEnv, const int64_t *off_d, const int64
     if (rc) return rc;
   }
   void *f = (void *)daa_kernel<T, DB>;
-  if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lay.total) != cudaSuccess) {
+  if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, ctx->smem_optin) != cudaSuccess) {
     ctx->err = "cudaFuncSetAttribute failed";
     return ACE_ERR_CUDA;
   }

@@ -61,6 +61,10 @@ static void type_sizes(const ace_ctx *ctx, int &sE, int &sG, bool &same) {
   }
 }
 
+// The maximum dynamic shared memory of a kernel is a process-wide attribute
+// of the function, shared by every context: it is set to the device's
+// opt-in limit (never lowered by a context with a smaller spec); each launch
+// passes its own size, and the occupancy queries use the context's size.
 int kernels_prepare(ace_ctx *ctx) {
   int sE, sG;
   bool same;
@@ -94,7 +98,7 @@ int kernels_prepare(ace_ctx *ctx) {
   int occ = 1;
   for (int g = 0; g < 2; ++g) {
     void *f = ef_func(ctx, g == 1);
-    if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lay.total) != cudaSuccess) {
+    if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, ctx->smem_optin) != cudaSuccess) {
       ctx->err = "cudaFuncSetAttribute failed";
       return ACE_ERR_CUDA;
     }
@@ -106,7 +110,7 @@ int kernels_prepare(ace_ctx *ctx) {
   EFLayout la = ef_layout(ctx->ntab, nRs, ctx->L, ctx->nA, ctx->aa_chunk, 1, 0, 256, sE, sE, true);
   ctx->aa_smem = la.total;
   void *fa = aa_func(ctx);
-  if (cudaFuncSetAttribute(fa, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)la.total) != cudaSuccess) {
+  if (cudaFuncSetAttribute(fa, cudaFuncAttributeMaxDynamicSharedMemorySize, ctx->smem_optin) != cudaSuccess) {
     ctx->err = "cudaFuncSetAttribute failed";
     return ACE_ERR_CUDA;
   }
@@ -118,7 +122,7 @@ int kernels_prepare(ace_ctx *ctx) {
   EFLayout lu = ef_layout(ctx->ntab, nRs, ctx->L, ctx->nA, ctx->ub_chunk, 1, 0, 128, sE, sE, true);
   ctx->ub_smem = lu.total;
   void *fu = ub_func(ctx);
-  if (cudaFuncSetAttribute(fu, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lu.total) != cudaSuccess) {
+  if (cudaFuncSetAttribute(fu, cudaFuncAttributeMaxDynamicSharedMemorySize, ctx->smem_optin) != cudaSuccess) {
     ctx->err = "cudaFuncSetAttribute failed";
     return ACE_ERR_CUDA;
   }
@@ -140,7 +144,7 @@ int launch_energy_forces(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const d
   void *f = ef_func(ctx, G != nullptr);
   if (cpx) {
     f = ef_func_cplx(ctx, G != nullptr);
-    if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ctx->smem) != cudaSuccess) {
+    if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, ctx->smem_optin) != cudaSuccess) {
       ctx->err = "cudaFuncSetAttribute failed";
       return ACE_ERR_CUDA;
     }

@@ -680,7 +680,7 @@ int mlp_prepare(ace_ctx *ctx) {
   ctx->mlp_tc = ctx->mlpD <= TC_K1 && ctx->mlpC <= TC_N3 && ctx->mlpC % 4 == 0 &&
                 !(menv && std::string(menv) == "fp32");
   if (ctx->mlp_tc) {
-    if (cudaFuncSetAttribute(mlp_fwd_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TCSmem)) !=
+    if (cudaFuncSetAttribute(mlp_fwd_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, ctx->smem_optin) !=
         cudaSuccess) {
       ctx->err = "cudaFuncSetAttribute failed";
       return ACE_ERR_CUDA;
@@ -698,9 +698,9 @@ int mlp_prepare(ace_ctx *ctx) {
     ctx->err = "radial MLP too large for shared memory";
     return ACE_ERR_UNSUPPORTED;
   }
-  if (cudaFuncSetAttribute(mlp_fwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ctx->mlp_smem_f) !=
+  if (cudaFuncSetAttribute(mlp_fwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, ctx->smem_optin) !=
           cudaSuccess ||
-      cudaFuncSetAttribute(mlp_bwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ctx->mlp_smem_b) !=
+      cudaFuncSetAttribute(mlp_bwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, ctx->smem_optin) !=
           cudaSuccess) {
     ctx->err = "cudaFuncSetAttribute failed";
     return ACE_ERR_CUDA;

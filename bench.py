@@ -277,10 +277,16 @@ def run_learned(args, torch, dist, rank, world, local):
     t0 = time.perf_counter()
     psteps = X["pretrain_steps"] if args.pretrain_steps is None else args.pretrain_steps
     dsteps = X["distill_steps"] if args.distill_steps is None else args.distill_steps
-    LR.pretrain_radial(ctx, mlp, spec, nsamples=X["neighbour_samples"], steps=psteps)
+    LR.pretrain_radial(ctx, mlp, spec, nsamples=X["neighbour_samples"], steps=psteps,
+                       teacher=None if args.plain_pretrain else teacher_spec)
     c0 = LR.fit_coefficients(ctx, spec, LR.sub_batch(train, 0, 20000), Etr[:20000], forces=forces)
     ctx.set_params(c0)
     t1 = time.perf_counter()
+    # the method without the network: the student spec's own species-blind
+    # polynomial radials of width K, coefficients fitted the same way
+    plain_student = Context(spec, "fp32", device=local)
+    cp = LR.fit_coefficients(plain_student, spec, LR.sub_batch(train, 0, 20000), Etr[:20000], forces=forces)
+    plain_student.set_params(cp)
     # judge on the held-out set: FP64 plain evaluation (device path, chunked)
     off_d = torch.from_numpy(ev.offsets).to(dev)
     rr_d = torch.from_numpy(ev.rr).to(dev)
@@ -297,6 +303,11 @@ def run_learned(args, torch, dist, rank, world, local):
         e["F_rel_rmse"] = float(np.sqrt(np.mean((G - Gref) ** 2)) / np.sqrt(np.mean(Gref ** 2)))
         return e
     err_untrained = judged()
+    plain_student.energy_forces_device(off_d, rr_d, sp_d, E_d, G_d)
+    Ep, Gp = E_d.cpu().numpy(), G_d.cpu().numpy()
+    err_no_network = LR.energy_error(Ep, Eref)
+    err_no_network["F_rel_rmse"] = float(np.sqrt(np.mean((Gp - Gref) ** 2)) / np.sqrt(np.mean(Gref ** 2)))
+    del plain_student
     c1, hist = LR.distill(ctx, mlp, spec, train, Etr, c0, steps=dsteps, batch_envs=512, lr=1e-3,
                           refit_every=500, refit_envs=20000, forces=forces)
     t2 = time.perf_counter()
@@ -356,6 +367,7 @@ def run_learned(args, torch, dist, rank, world, local):
                        "teacher": {"nA": teacher_spec.nA, "nAA": teacher_spec.nAA, "nB": teacher_spec.nB},
                        "l2": "flushed (256 MB write) between timed steps"},
             "error_vs_plain_fp64": err, "error_untrained_student": err_untrained,
+            "error_without_network": err_no_network,
             "training": {"neighbour_samples": X["neighbour_samples"], "pretrain_steps": psteps,
                          "train_envs": X["train_envs"], "distill_steps": dsteps,
                          "force_envs": nf if fw > 0 else 0, "force_weight": fw,
@@ -386,6 +398,8 @@ def main():
     ap.add_argument("--force-weight", type=float, default=None, help="learned form: weight of gradient rows")
     ap.add_argument("--pretrain-steps", type=int, default=None, help="learned form: radial pretraining steps")
     ap.add_argument("--distill-steps", type=int, default=None, help="learned form: distillation steps")
+    ap.add_argument("--plain-pretrain", action="store_true",
+                    help="learned form: pretrain on the species-blind polynomial radials")
     ap.add_argument("--workload", default="ord4_deg12", choices=sorted(WORKLOADS) + ["learned_4sp"])
     args = ap.parse_args()
     global WORKLOAD

@@ -440,3 +440,20 @@ def test_host_pipeline_species(lib):
     bad[b.offsets[11000]] = 5
     with pytest.raises(lib.AceError):
         ctx.energy_forces(b.offsets, b.rr, bad)
+
+
+def test_contexts_of_different_sizes_interleave(lib, oracle_mod):
+    """Contexts of one precision with different spec sizes (so different
+    shared-memory needs) can be created and used in any order."""
+    big = get_spec("cfg2")
+    small = get_spec("test")
+    cb = lib.Context(big, "fp32x2"); cb.set_params(random_coefficients(big, seed=1))
+    cs = lib.Context(small, "fp32x2"); cs.set_params(random_coefficients(small, seed=1))
+    b = random_batch(20, 10, 30, seed=4)
+    Eb1, _ = cb.energy_forces(b.offsets, b.rr)
+    Bb1 = cb.basis(b.offsets, b.rr)
+    cs.energy_forces(b.offsets, b.rr)
+    cs.basis(b.offsets, b.rr)
+    Eb2, _ = cb.energy_forces(b.offsets, b.rr)        # after the smaller context's set-up
+    Bb2 = cb.basis(b.offsets, b.rr)
+    assert np.array_equal(Eb1, Eb2) and np.array_equal(Bb1, Bb2)
