@@ -358,3 +358,35 @@ def vector_rpe_basis(ll: tuple, pattern: tuple) -> np.ndarray:
     rk = int(np.sum(S > 1e-7 * S[0]))
     Wr = np.diag(np.sqrt(S[:rk])) @ U[:, :rk].T @ W
     return (Wr[:, :half] + 1j * Wr[:, half:]).reshape(rk, 3, nM)
+
+
+@lru_cache(maxsize=None)
+def rpe_basis_L(ll: tuple, pattern: tuple, L: int) -> np.ndarray:
+    """``rpe_basis`` for a spherical-tensor output of total angular momentum L
+    (SphericalVector, src/properties.jl:431-520): the coupling-tree rows
+    ending in L (``coupling_tree_L``) over ``mrange_L(ll, L)``, symmetrised
+    with the permutation Gramian (SVD, rank rtol 1e-7).  Row b defines the
+    components B_b^M = sum_{sum mm = M} U[b, mm] prod Y_{l_t m_t}, which
+    rotate like Y_L^M."""
+    Ure = coupling_tree_L(ll, L)
+    mm = mrange_L(ll, L)
+    nre = Ure.shape[0]
+    if nre == 0 or mm.shape[0] == 0:
+        return np.zeros((0, mm.shape[0]))
+    N = len(ll)
+    lmax = max(ll)
+    base = 2 * lmax + 1
+    w = base ** np.arange(N)
+    keys = ((mm + lmax) * w).sum(axis=1)
+    order = np.argsort(keys)
+    skeys = keys[order]
+    G = np.zeros((nre, nre))
+    for sig in stabiliser(pattern, ll):
+        pk = ((mm[:, list(sig)] + lmax) * w).sum(axis=1)
+        idx = order[np.searchsorted(skeys, pk)]
+        G += Ure @ Ure[:, idx].T
+    U, S, _ = np.linalg.svd(G)
+    if S.size == 0 or S[0] <= 0:
+        return np.zeros((0, mm.shape[0]))
+    rk = int(np.sum(S > 1e-7 * S[0]))
+    return np.diag(np.sqrt(S[:rk])) @ U[:, :rk].T @ Ure

@@ -189,5 +189,42 @@ class LinearVectorModel:
         return parts[0] if single else parts
 
 
-__all__ = ["ACEConfig", "SymmetricBasis", "LinearACEModel", "LinearVectorModel", "random_coefficients",
-           "symmetric_basis"]
+class LinearSphericalModel:
+    """A linear model over a SphericalVector{L} basis (``spec.spherical_basis``):
+    V_M(cfg) = sum_b c_b B_b^M(cfg), complex, M = -L..L.  Evaluated as
+    2 (2L+1) complex-coefficient properties: Re V_M with c~^M and
+    Im V_M = Re(-i c~^M . AA)."""
+
+    def __init__(self, spec, c, precision: str = "fp64", device: int = 0):
+        self.spec = spec
+        self.L = spec.Lout
+        self.c = np.array(c, dtype=np.float64)
+        self.ctx = Context(spec, precision, device)
+        self.set_params(self.c)
+
+    def set_params(self, c):
+        self.c[...] = c
+        ct = self.spec.ctilde_spherical(self.c).astype(np.complex128)
+        self.ctx.set_ctilde_complex(np.concatenate([ct, -1j * ct]))
+        return self
+
+    def _eval(self, cfgs):
+        single, off, rr, sp = _pack(cfgs)
+        E, G = self.ctx.energy_forces_multi(off, rr, sp)      # (nEnv, 2n), (nNbr, 2n, 3)
+        n = 2 * self.L + 1
+        return single, off, E[:, :n] + 1j * E[:, n:], G[:, :n] + 1j * G[:, n:]
+
+    def evaluate(self, cfgs):
+        """V (2L+1,) complex per configuration."""
+        single, _, V, _ = self._eval(cfgs)
+        return V[0] if single else V
+
+    def grad_config(self, cfgs):
+        """dV_M/drr_j[a] as (J, 2L+1, 3) complex per configuration."""
+        single, off, _, G = self._eval(cfgs)
+        parts = [G[off[e]:off[e + 1]] for e in range(len(off) - 1)]
+        return parts[0] if single else parts
+
+
+__all__ = ["ACEConfig", "SymmetricBasis", "LinearACEModel", "LinearVectorModel", "LinearSphericalModel",
+           "random_coefficients", "symmetric_basis"]

@@ -88,8 +88,10 @@ def gensparse_ordered(deg: np.ndarray, ls: np.ndarray, ms: np.ndarray,
     assert np.all(np.diff(deg) >= 0), "A spec must be sorted by degree"
     nA = len(deg)
     vec = prop == "vector"
-    mslack = 1 if vec else 0
-    out = [np.zeros((0 if vec else 1, 0), dtype=np.int64)]  # order 0: the constant (invariants only)
+    sphL = prop[1] if isinstance(prop, tuple) and prop[0] == "spherical" else None
+    mslack = 1 if vec else (sphL if sphL is not None else 0)
+    const = not vec and (sphL is None or sphL == 0)
+    out = [np.zeros((1 if const else 0, 0), dtype=np.int64)]  # order 0: the constant (L = 0 outputs only)
     for k in range(1, maxorder + 1):
         # rows: partial tuples, their degree sum and m sum
         tup = np.zeros((1, 0), dtype=np.int64)
@@ -119,6 +121,9 @@ def gensparse_ordered(deg: np.ndarray, ls: np.ndarray, ms: np.ndarray,
             tup, dsum, msum, lsum = tup[keep], dsum[keep], msum[keep], lsum[keep]
         if vec and len(tup):
             tup = tup[(lsum % 2 == 1) & (np.abs(msum) <= 1)]
+        elif sphL is not None and len(tup):
+            if k >= 2 or sphL > 0:
+                tup = tup[(lsum % 2 == sphL % 2) & (np.abs(msum) <= sphL)]
         elif k >= 2 and len(tup):
             keep = (lsum % 2 == 0) & (msum == 0)
             tup = tup[keep]
@@ -399,6 +404,127 @@ def vector_basis(maxorder: int, maxdeg: float, nR: int | None = None, maxL: int 
     return VectorSpec(radial=radial, maxL=maxL, nspecies=nspecies, aspec=aspec, orders=orders, iAA2iA=iAA2iA,
                       U=sp.csr_matrix((0, len(orders))), Bdeg=np.array(Bdeg), Bclass=np.array(Bclass), info=info,
                       Uvec=Uvec)
+
+
+@dataclass
+class SphericalSpec(ACESpec):
+    """A SphericalVector{L} basis: complex components B_b^M = sum_k
+    U_M[b, k] AA_k, M = -L..L, rotating like Y_L^M (src/properties.jl:431-520);
+    Usph = (U_{-L}, ..., U_L), real CSR (nB x nAA)."""
+    Usph: tuple = ()
+    Lout: int = 0
+
+    @property
+    def nB(self):
+        return self.Usph[0].shape[0]
+
+    def ctilde_spherical(self, c: np.ndarray) -> np.ndarray:
+        """c~^M = U_M^T c, real (2L+1, nAA)."""
+        c = np.asarray(c, dtype=np.float64)
+        return np.stack([np.asarray(Um.T @ c).ravel() for Um in self.Usph])
+
+
+def spherical_basis(L: int, maxorder: int, maxdeg: float, nR: int | None = None, maxL: int | None = None,
+                    nspecies: int = 1, r0: float = 1.0, rcut: float = 5.0, rin: float | None = None,
+                    pcut: int = 2, pin: int = 0, p: int = 2, zero_tol: float = 1e-12) -> SphericalSpec:
+    """SymmetricBasis(SphericalVector(L), ...): AA tuples with sum(l) of the
+    parity of L and |sum(m)| <= L (src/properties.jl:470-480), per class the
+    coupling tree ended in L, permutation-symmetrised (``rpe_basis_L``),
+    cleaned as ``symmetric_basis`` cleans.  Parity of U unpinned against the
+    reference's SVD rotation, as for invariants."""
+    from .coupling import mrange_L, rpe_basis_L
+    if nR is None:
+        nR = int(maxdeg)
+    if maxL is None:
+        maxL = int(maxdeg)
+    radial = rn_basis(maxdeg=nR, r0=r0, rcut=rcut, rin=rin, pcut=pcut, pin=pin, p=p)
+    aspec = init1pspec(nR, maxL, maxdeg, nspecies)
+    nA0 = len(aspec)
+    per_order = gensparse_ordered(aspec.degree.astype(np.float64), aspec.l, aspec.m, maxorder, maxdeg,
+                                  prop=("spherical", L))
+    rows, orders = [], []
+    for k, tup in enumerate(per_order):
+        if len(tup) == 0:
+            continue
+        r = -np.ones((len(tup), maxorder), dtype=np.int64)
+        r[:, :k] = tup[:, ::-1]
+        rows.append(r)
+        orders.append(np.full(len(tup), k, dtype=np.int64))
+    iAA2iA = np.concatenate(rows, axis=0)
+    orders = np.concatenate(orders)
+    nAA0 = len(orders)
+    base = nA0 + 1
+    keys = _encode(iAA2iA, base)
+    korder = np.argsort(keys)
+    skeys = keys[korder]
+    aidx = -np.ones((nspecies, nR + 1, maxL + 1, 2 * maxL + 1), dtype=np.int64)
+    aidx[aspec.mu, aspec.n, aspec.l, aspec.m + maxL] = np.arange(nA0)
+    a_m = aspec.m
+    refmask = np.all(np.where(iAA2iA >= 0, a_m[np.maximum(iAA2iA, 0)] == 0, True), axis=1)
+    Irow, Jcol, vals, Bdeg, Bclass = [], [], [], [], []
+    nB = 0
+    nclass = 0
+    for iAA in np.nonzero(refmask)[0]:
+        k = int(orders[iAA])
+        vs = iAA2iA[iAA, :k]
+        if k == 0:
+            if L != 0:
+                continue
+            Irow.append(np.array([nB])); Jcol.append(np.array([iAA])); vals.append(np.array([[1.0]]).T[:, :1].T)
+            Bdeg.append(0.0); Bclass.append(nclass)
+            nB += 1; nclass += 1
+            continue
+        ll = tuple(int(x) for x in aspec.l[vs])
+        nn = tuple((int(a), int(b)) for a, b in zip(aspec.mu[vs], aspec.n[vs]))
+        U = rpe_basis_L(ll, _nn_pattern(nn), L)                 # (nb, nM)
+        if U.shape[0] == 0:
+            continue
+        mm = mrange_L(ll, L)
+        M = mm.sum(axis=1)
+        A = np.stack([aidx[aspec.mu[vs[t]], aspec.n[vs[t]], ll[t], mm[:, t] + maxL] for t in range(k)], axis=1)
+        if np.any(A < 0):
+            raise RuntimeError("m-tuple outside the 1p basis")
+        A = -np.sort(-A, axis=1)
+        r = -np.ones((len(A), maxorder), dtype=np.int64)
+        r[:, :k] = A
+        pk = _encode(r, base)
+        pos = np.searchsorted(skeys, pk)
+        if np.any(pos >= len(skeys)) or np.any(skeys[np.minimum(pos, len(skeys) - 1)] != pk):
+            raise RuntimeError("bcol_ordered not in AA-spec")
+        cols = korder[pos]
+        ucols, inv = np.unique(cols, return_inverse=True)
+        Uc = np.zeros((U.shape[0], 2 * L + 1, len(ucols)))
+        for Mi in range(2 * L + 1):
+            sel = M == Mi - L
+            np.add.at(Uc[:, Mi, :].T, inv[sel], U[:, sel].T)
+        rmax = np.abs(Uc).max(axis=(1, 2), keepdims=True)
+        Uc[np.abs(Uc) <= zero_tol * rmax] = 0.0
+        d = float(sum(aspec.degree[vs]))
+        for irow in range(U.shape[0]):
+            nzm = np.any(Uc[irow] != 0, axis=0)
+            Irow.append(np.full(int(nzm.sum()), nB)); Jcol.append(ucols[nzm]); vals.append(Uc[irow][:, nzm])
+            Bdeg.append(d); Bclass.append(nclass)
+            nB += 1
+        nclass += 1
+    Irow = np.concatenate(Irow); Jcol = np.concatenate(Jcol); V = np.concatenate(vals, axis=1)
+    Ufull = [sp.csr_matrix((V[i], (Irow, Jcol)), shape=(nB, nAA0)) for i in range(2 * L + 1)]
+    colnorm = sum(np.asarray(abs(Ui).sum(axis=0)).ravel() for Ui in Ufull)
+    Inz = np.nonzero(colnorm > 0.0)[0]
+    Usph = tuple(Ui[:, Inz].tocsr() for Ui in Ufull)
+    iAA2iA = iAA2iA[Inz]
+    orders = orders[Inz]
+    used = np.zeros(nA0, dtype=bool)
+    used[iAA2iA[iAA2iA >= 0]] = True
+    new_inds = -np.ones(nA0, dtype=np.int64)
+    new_inds[used] = np.arange(used.sum())
+    iAA2iA = np.where(iAA2iA >= 0, new_inds[np.maximum(iAA2iA, 0)], -1)
+    aspec = OnePSpec(aspec.mu[used], aspec.n[used], aspec.l[used], aspec.m[used])
+    info = dict(nA_pre=nA0, nAA_pre=nAA0, nclass=nclass, prop=f"spherical{L}",
+                nAA_by_order={int(k): int((orders == k).sum()) for k in np.unique(orders)},
+                maxorder=maxorder, maxdeg=maxdeg, nR=nR, maxL=maxL, nspecies=nspecies)
+    return SphericalSpec(radial=radial, maxL=maxL, nspecies=nspecies, aspec=aspec, orders=orders, iAA2iA=iAA2iA,
+                         U=sp.csr_matrix((0, len(orders))), Bdeg=np.array(Bdeg), Bclass=np.array(Bclass),
+                         info=info, Usph=Usph, Lout=L)
 
 
 def random_coefficients(spec: ACESpec, seed: int = 0) -> np.ndarray:

@@ -90,3 +90,34 @@ def test_vector_model_after_autotune_to_trie(lib, vmodel_inputs, monkeypatch):
     b = random_batch(20, 8, 16, seed=2)
     cfgs = [b.rr[b.offsets[e]:b.offsets[e + 1]] for e in range(b.nenv)]
     assert np.allclose(model.evaluate(cfgs), ref.evaluate(cfgs), rtol=1e-12, atol=1e-14)
+
+
+@pytest.mark.parametrize("L", [1, 2])
+def test_spherical_model(lib, oracle_mod, L):
+    """SphericalVector{L} models (complex components) against the host
+    evaluation sum_b c_b B_b^M from the oracle's A, and finite differences."""
+    from ace_gb300.model import LinearSphericalModel
+    from ace_gb300.spec import spherical_basis
+    spec = spherical_basis(L, 3, 7, maxL=5)
+    c = random_coefficients(spec, seed=3)
+    model = LinearSphericalModel(spec, c, precision="fp64")
+    b = random_batch(40, 6, 18, seed=4)
+    cfgs = [b.rr[b.offsets[e]:b.offsets[e + 1]] for e in range(b.nenv)]
+    V = model.evaluate(cfgs)                                   # (nEnv, 2L+1) complex
+    orc = oracle_mod.Oracle(spec, ctilde=np.zeros(spec.nAA))
+    A = orc.A(b.offsets, b.rr)
+    AA = np.ones((A.shape[0], spec.nAA), dtype=complex)
+    for t in range(spec.maxorder):
+        v = spec.iAA2iA[:, t]
+        AA = AA * np.where(v >= 0, A[:, np.maximum(v, 0)], 1.0)
+    Vref = AA @ spec.ctilde_spherical(c).T
+    assert np.max(np.abs(V - Vref)) <= 1e-12 * np.max(np.abs(Vref))
+    G = model.grad_config(cfgs)
+    h = 1e-5
+    x = cfgs[3]
+    for j in (0, len(x) - 1):
+        for a in range(3):
+            xp = x.copy(); xp[j, a] += h
+            xm = x.copy(); xm[j, a] -= h
+            fd = (model.evaluate(xp) - model.evaluate(xm)) / (2 * h)
+            assert np.allclose(G[3][j, :, a], fd, rtol=1e-6, atol=1e-7 * np.max(np.abs(V)))

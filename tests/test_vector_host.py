@@ -65,3 +65,46 @@ def test_linear_independence(oracle_mod, vspec):
     M = B.transpose(0, 2, 1).reshape(-1, vspec.nB)
     s = np.linalg.svd(M, compute_uv=False)
     assert s[-1] / s[0] > 1e-10
+
+
+# ---------------------------------------------------------------- SphericalVector{L}
+
+def spherical_B(oracle_mod, spec, offsets, rr):
+    orc = oracle_mod.Oracle(spec, ctilde=np.zeros(spec.nAA))
+    A = orc.A(offsets, rr)
+    AA = np.ones((A.shape[0], spec.nAA), dtype=complex)
+    for t in range(spec.maxorder):
+        v = spec.iAA2iA[:, t]
+        AA = AA * np.where(v >= 0, A[:, np.maximum(v, 0)], 1.0)
+    return np.stack([AA @ Um.T.toarray() for Um in spec.Usph], axis=2)   # (nEnv, nB, 2L+1)
+
+
+def wigner_from_sh(oracle_mod, L, Q):
+    """D with Y_L(Q x) = D Y_L(x), from the oracle's spherical harmonics."""
+    rng = np.random.default_rng(0)
+    X = rng.standard_normal((40, 3))
+    def YL(x):
+        return np.asarray(oracle_mod.sh(L, x))[L * L:(L + 1) ** 2]
+    A = np.stack([YL(x) for x in X])                    # (n, 2L+1)
+    Bq = np.stack([YL(Q @ x) for x in X])
+    D, *_ = np.linalg.lstsq(A, Bq, rcond=None)
+    return D.T
+
+
+@pytest.mark.parametrize("L", [0, 1, 2])
+def test_spherical_equivariance(oracle_mod, L):
+    from ace_gb300.spec import spherical_basis
+    spec = spherical_basis(L, 3, 6, maxL=4)
+    b = random_batch(5, 5, 9, seed=11)
+    B = spherical_B(oracle_mod, spec, b.offsets, b.rr)
+    assert np.max(np.abs(B)) > 1e-3
+    for Q in (_rotation(1), _rotation(6)):
+        D = wigner_from_sh(oracle_mod, L, Q)
+        BQ = spherical_B(oracle_mod, spec, b.offsets, b.rr @ Q.T)
+        assert np.allclose(BQ, B @ D.T, rtol=1e-9, atol=1e-9 * np.max(np.abs(B)))
+    # inversion: (-1)^L
+    Bi = spherical_B(oracle_mod, spec, b.offsets, -b.rr)
+    assert np.allclose(Bi, (-1) ** L * B, rtol=1e-10, atol=1e-10 * np.max(np.abs(B)))
+    if L == 0:
+        from ace_gb300.spec import symmetric_basis
+        assert spec.nB == symmetric_basis(3, 6, maxL=4).nB
