@@ -204,6 +204,12 @@ __device__ __forceinline__ void build_A(const EFArgs &a, const Tables<T> &tb, in
   __syncthreads();
 }
 
+// Re(a b)
+template <typename T> __device__ __forceinline__ T re_mul(cpx<T> a, cpx<T> b) { return a.re * b.re - a.im * b.im; }
+#if ACE_DF_DOT2
+template <> __device__ __forceinline__ df re_mul<df>(cpx<df> a, cpx<df> b) { return dot2(a.re, b.re, -a.im, b.im); }
+#endif
+
 template <typename T> __device__ __forceinline__ cpx<T> shfl_down_c(cpx<T> v, int off) {
   return {__shfl_down_sync(0xffffffffu, v.re, off), __shfl_down_sync(0xffffffffu, v.im, off)};
 }
@@ -392,7 +398,7 @@ __global__ void __launch_bounds__(NT) ef_kernel(EFArgs a) {
         }
 #pragma unroll
         for (int u = 0; u < IU; ++u)
-          if (P[u] > 0) eacc = eacc + (bar[u].re * H[u].re - bar[u].im * H[u].im);
+          if (P[u] > 0) eacc = eacc + re_mul<TE>(bar[u], H[u]);
         if (GRAD) {
           cpx<TG> v[IU][KP];
 #pragma unroll

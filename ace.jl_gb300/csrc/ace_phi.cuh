@@ -15,6 +15,12 @@
 
 #include "ace_arith.cuh"
 
+// double-float complex products through dot2 (one renormalisation per
+// component) instead of four products and two sums
+#ifndef ACE_DF_DOT2
+#define ACE_DF_DOT2 1
+#endif
+
 namespace ace {
 
 template <typename T> struct cpx { T re, im; };
@@ -22,6 +28,11 @@ template <typename T> struct cpx { T re, im; };
 template <typename T> __device__ __forceinline__ cpx<T> cmul(cpx<T> a, cpx<T> b) {
   return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
 }
+#if ACE_DF_DOT2
+template <> __device__ __forceinline__ cpx<df> cmul<df>(cpx<df> a, cpx<df> b) {
+  return {dot2(a.re, b.re, -a.im, b.im), dot2(a.re, b.im, a.im, b.re)};
+}
+#endif
 template <typename T> __device__ __forceinline__ cpx<T> cadd(cpx<T> a, cpx<T> b) {
   return {a.re + b.re, a.im + b.im};
 }
