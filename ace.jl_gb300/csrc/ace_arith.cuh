@@ -70,6 +70,20 @@ __device__ __forceinline__ df dot2(df a, df b, df c, df d) {
   fast_two_sum(s, e, h, l);
   return {h, l};
 }
+// a*b + c with one renormalisation (15 FP32 operations instead of 18)
+__device__ __forceinline__ df fma_df(df a, df b, df c) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  float s, t;
+  two_sum(p, c.hi, s, t);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  e = __fadd_rn(e, c.lo);
+  e = __fadd_rn(e, t);
+  float h, l;
+  fast_two_sum(s, e, h, l);
+  return {h, l};
+}
 __device__ __forceinline__ df operator/(df a, df b) {
   const float q1 = __fdiv_rn(a.hi, b.hi);
   const df r = a - b * q1;

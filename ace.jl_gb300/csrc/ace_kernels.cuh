@@ -196,7 +196,7 @@ __device__ __forceinline__ void build_A(const EFArgs &a, const Tables<T> &tb, in
         if (a.nspecies > 1 && ssp[q] != mu) continue;
         const T *sl = slab + (size_t)q * SE;
         const cpx<T> Y = ((const cpx<T> *)(sl + a.nRs))[iy];
-        acc = cadd(acc, cscale(Y, sl[n]));
+        acc = cfma(acc, Y, sl[n]);
       }
       A[i] = acc;
     }
@@ -392,7 +392,7 @@ __global__ void __launch_bounds__(NT) ef_kernel(EFArgs a) {
             cli[u][g] = (CPX && ok) ? load_coef<TE>(a.ic, (int64_t)(ITEM_G + 2 + g) * a.in + f) : ze;
             if (g < nl[u]) {
               if constexpr (CPX) H[u] = cadd(H[u], cmul(AE[ul[u][g]], cpx<TE>{cl[u][g], cli[u][g]}));
-              else H[u] = cadd(H[u], cscale(AE[ul[u][g]], cl[u][g]));
+              else H[u] = cfma(H[u], AE[ul[u][g]], cl[u][g]);
             }
           }
         }
@@ -681,7 +681,7 @@ __global__ void __launch_bounds__(128) ub_fused_kernel(EFArgs a, const uint4 *ur
         }
       }
 #pragma unroll
-      for (int i = 0; i < UB_R; ++i) acc[i] = acc[i] + load_coef<TE>(uval, slot * UB_R + i) * p.re;
+      for (int i = 0; i < UB_R; ++i) acc[i] = fmag(load_coef<TE>(uval, slot * UB_R + i), p.re, acc[i]);
       if ((rc.w >> 30) & 1u) {
         // write the group's r rows; the accumulators shift down so that only
         // r conversions to double (FP64-pipe work on GB300) are issued

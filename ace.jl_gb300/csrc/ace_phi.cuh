@@ -39,6 +39,22 @@ template <typename T> __device__ __forceinline__ cpx<T> cadd(cpx<T> a, cpx<T> b)
 template <typename T> __device__ __forceinline__ cpx<T> cscale(cpx<T> a, T s) {
   return {a.re * s, a.im * s};
 }
+// a b + c d and a b + c, fused in double-float
+template <typename T> __device__ __forceinline__ T dot2g(T a, T b, T c, T d) { return a * b + c * d; }
+template <typename T> __device__ __forceinline__ T fmag(T a, T b, T c) { return a * b + c; }
+#if ACE_DF_DOT2
+template <> __device__ __forceinline__ df dot2g<df>(df a, df b, df c, df d) { return dot2(a, b, c, d); }
+template <> __device__ __forceinline__ df fmag<df>(df a, df b, df c) { return fma_df(a, b, c); }
+#endif
+// acc + a s (real s)
+template <typename T> __device__ __forceinline__ cpx<T> cfma(cpx<T> acc, cpx<T> a, T s) {
+  return cadd(acc, cscale(a, s));
+}
+#if ACE_DF_DOT2
+template <> __device__ __forceinline__ cpx<df> cfma<df>(cpx<df> acc, cpx<df> a, df s) {
+  return {fma_df(a.re, s, acc.re), fma_df(a.im, s, acc.im)};
+}
+#endif
 
 __host__ __device__ constexpr int size_p(int L) { return (L + 1) * (L + 2) / 2; }
 __host__ __device__ constexpr int size_y(int L) { return (L + 1) * (L + 1); }
@@ -97,8 +113,8 @@ __device__ __forceinline__ void radial_eval(const Tables<T> &tb, T r, T *R, T *d
   R[1] = al * R[0];
   if (GRAD) { dP1 = al * dP0 + tb.rA[1] * R[0]; dR[1] = dP1 * dtdr; }
   for (int n = 2; n < tb.nR; ++n) {
-    al = tb.rA[n] * t + tb.rB[n];
-    R[n] = al * R[n - 1] + tb.rC[n] * R[n - 2];
+    al = fmag(tb.rA[n], t, tb.rB[n]);
+    R[n] = dot2g(al, R[n - 1], tb.rC[n], R[n - 2]);
     if (GRAD) {
       const T dP2 = al * dP1 + tb.rC[n] * dP0 + tb.rA[n] * R[n - 1];
       dR[n] = dP2 * dtdr;
@@ -148,7 +164,7 @@ __device__ __forceinline__ void sh_col_values(const Tables<T> &tb, const Angles<
     T p;
     if (l == m) p = pmm;
     else if (l == m + 1) p = g.cost * tb.alpC[l] * pmm;
-    else p = tb.alpA[idx_p(l, m)] * (g.cost * p1 + tb.alpB[idx_p(l, m)] * p2);
+    else p = tb.alpA[idx_p(l, m)] * dot2g(g.cost, p1, tb.alpB[idx_p(l, m)], p2);
     if (l > m) { p2 = p1; p1 = p; }
     if (m == 0) {
       Y[idx_y(l, 0)] = {p * tb.invsqrt2, zero};
