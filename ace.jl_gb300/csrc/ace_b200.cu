@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <functional>
 #include <string>
@@ -590,7 +591,8 @@ static int drive(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, const doubl
 }
 
 // Host buffers in and out, large batches: the batch is cut into chunks of
-// environments; chunk k+1 is validated on the host while chunk k's positions
+// environments (up to 8; ACE_B200_PIPE_CHUNKS overrides); chunk k+1 is
+// validated on the host while chunk k's positions
 // are copied in (copy stream), evaluated (compute stream) and its energies and
 // gradients copied out (a second copy stream), so copies, host checks and
 // kernels overlap.  An invalid chunk stops the pipeline; earlier chunks may
@@ -616,7 +618,9 @@ static int energy_forces_pipelined(ace_ctx *ctx, int64_t nEnv, const int64_t *of
   const int nsp = input_species(ctx);
   if (nsp > 1 && !sp) return ctx_fail(ctx, ACE_ERR_INVALID, "species required for a multi-species spec");
   const bool wsp = sp && nsp > 1;
-  const int nchunk = (int)std::max<int64_t>(2, std::min<int64_t>(16, nEnv / PIPE_MIN_CHUNK));
+  int maxchunk = 8;  // measured on GB300 (ord4/deg12, 100k envs): 4 / 8 / 16 / 32 chunks -> 2.74 / 2.82 / 2.74 / 2.68 M env/s
+  if (const char *pc = getenv("ACE_B200_PIPE_CHUNKS")) maxchunk = std::max(2, std::min(64, atoi(pc)));
+  const int nchunk = (int)std::max<int64_t>(2, std::min<int64_t>(maxchunk, nEnv / PIPE_MIN_CHUNK));
   ACE_CUDA(cudaSetDevice(ctx->device));
   if ((rc = ensure_pipeline(ctx, nchunk))) return rc;
   size_t need = 0;
