@@ -347,7 +347,9 @@ __global__ void __launch_bounds__(NT) ef_kernel(EFArgs a) {
       // latency of the dependent double-float arithmetic
       constexpr int KP = (K > 1) ? K - 1 : 1;
       constexpr int IU = EF_ITEM_ILP;
+#if !EF_ITEM_RUNS
       const int lane = tid & 31;
+#endif
       const cpx<TG> gone = {TG(1), TG(0)};
       const TE ze = Arith<TE>::zero();
 #if EF_ITEM_RUNS
@@ -403,24 +405,27 @@ __global__ void __launch_bounds__(NT) ef_kernel(EFArgs a) {
           cpx<TG> v[IU][KP];
 #pragma unroll
           for (int u = 0; u < IU; ++u) {
-            cpx<TG> pre[KP], suf[KP];
-            pre[0] = gone;
-#pragma unroll
-            for (int d = 1; d < KP; ++d) pre[d] = (d < P[u]) ? cmul(pre[d - 1], aG[u][d - 1]) : pre[d - 1];
-            suf[KP - 1] = gone;
-#pragma unroll
-            for (int d = KP - 2; d >= 0; --d) suf[d] = (d + 1 < P[u]) ? cmul(aG[u][d + 1], suf[d + 1]) : gone;
-            const cpx<TG> bG = cmul(pre[KP - 1], aG[u][KP - 1]);
             const cpx<TG> h = {lower<TG>(H[u].re), lower<TG>(H[u].im)};
+            cpx<TG> bG;
+            {
+              cpx<TG> pre[KP], suf[KP];
+              pre[0] = gone;
+#pragma unroll
+              for (int d = 1; d < KP; ++d) pre[d] = (d < P[u]) ? cmul(pre[d - 1], aG[u][d - 1]) : pre[d - 1];
+              suf[KP - 1] = gone;
+#pragma unroll
+              for (int d = KP - 2; d >= 0; --d) suf[d] = (d + 1 < P[u]) ? cmul(aG[u][d + 1], suf[d + 1]) : gone;
+              bG = cmul(pre[KP - 1], aG[u][KP - 1]);
+#pragma unroll
+              for (int d = 0; d < KP; ++d)
+                v[u][d] = (d < P[u]) ? cmul(cmul(pre[d], suf[d]), h) : cpx<TG>{TG(0), TG(0)};
+            }
 #pragma unroll
             for (int g = 0; g < ITEM_G; ++g)
               if (g < nl[u]) {
                 if constexpr (CPX) dacc(ul[u][g], cmul(bG, cpx<TG>{lower<TG>(cl[u][g]), lower<TG>(cli[u][g])}));
                 else dacc(ul[u][g], cscale(bG, lower<TG>(cl[u][g])));
               }
-#pragma unroll
-            for (int d = 0; d < KP; ++d)
-              v[u][d] = (d < P[u]) ? cmul(cmul(pre[d], suf[d]), h) : cpx<TG>{TG(0), TG(0)};
           }
 #if EF_ITEM_RUNS
 #pragma unroll
