@@ -35,3 +35,18 @@ def test_library_exports_declared_symbols():
 def test_python_binding_lists_exports():
     from ace_gb300 import lib
     assert set(lib.EXPORTED) <= set(declared_symbols())
+
+
+def test_header_compiles_as_c99(tmp_path):
+    """include/ace_b200.h is plain C: a C99 consumer that names every entry
+    point compiles with -Wall -Werror (the library is not linked or run)."""
+    import shutil
+    import subprocess
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not available")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    obj = str(tmp_path / "c_consumer.o")
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic", "-c",
+                        "-I", os.path.join(root, "include"), os.path.join(root, "tests", "host", "c_consumer.c"),
+                        "-o", obj], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
