@@ -120,11 +120,15 @@ inline __host__ __device__ EFLayout ef_layout(int ntab, int nR, int L, int nA, i
   return l;
 }
 
+// schedule coefficients and records are read-only for a launch: loaded
+// through the non-coherent read-only path
 template <typename T> __device__ __forceinline__ T load_coef(const void *p, int64_t i);
-template <> __device__ __forceinline__ float load_coef<float>(const void *p, int64_t i) { return ((const float *)p)[i]; }
-template <> __device__ __forceinline__ double load_coef<double>(const void *p, int64_t i) { return ((const double *)p)[i]; }
+template <> __device__ __forceinline__ float load_coef<float>(const void *p, int64_t i) { return __ldg((const float *)p + i); }
+template <> __device__ __forceinline__ double load_coef<double>(const void *p, int64_t i) {
+  return __ldg((const double *)p + i);
+}
 template <> __device__ __forceinline__ df load_coef<df>(const void *p, int64_t i) {
-  const float2 v = ((const float2 *)p)[i];
+  const float2 v = __ldg((const float2 *)p + i);
   return {v.x, v.y};
 }
 
@@ -370,7 +374,7 @@ __global__ void __launch_bounds__(NT) ef_kernel(EFArgs a) {
           const int64_t f = f0 + (int64_t)u * NT;
           // item_n is a multiple of NT, so `ok` is uniform across the CTA
           const bool ok = f < a.in;
-          const uint4 rc = ok ? a.irec[f] : make_uint4(0u, 0u, 0u, 0u);
+          const uint4 rc = ok ? __ldg(a.irec + f) : make_uint4(0u, 0u, 0u, 0u);
           P[u] = (rc.w >> 16) & 0xf;
           nl[u] = (rc.w >> 20) & 0xf;
           heads[u] = (rc.w >> 24) & 0xff;
@@ -673,7 +677,7 @@ __global__ void __launch_bounds__(128) ub_fused_kernel(EFArgs a, const uint4 *ur
     double *Be = B + e * nB;
     for (int64_t j = 0; j < ulen; ++j) {
       const int64_t slot = j * nt + tid;
-      const uint4 rc = urec[slot];
+      const uint4 rc = __ldg(urec + slot);
       if (!(rc.w >> 31)) break;  // padding only follows a thread's last entry
       const int ord = (rc.w >> 24) & 7;
       const uint32_t vw[3] = {rc.x, rc.y, rc.z};
