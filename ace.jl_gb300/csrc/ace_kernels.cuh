@@ -40,10 +40,13 @@ __host__ __device__ inline size_t al16(size_t x) { return (x + 15) & ~size_t(15)
 #ifndef EF_ITEM_ILP
 #define EF_ITEM_ILP 2
 #endif
-// minimum resident CTAs per SM requested from the register allocator (0:
-// no request).  Measured on GB300 with the fp32x2 form: 6 gives +11 % on
-// order 5 / degree 16 but -3 % on order 4 / degree 12; an explicit 1 lets the
-// allocator take 150-210 registers and costs a third of the throughput.
+// minimum resident CTAs per SM requested from the register allocator
+// (EF_MIN_BLOCKS > 0 overrides the per-type default of ef_min_blocks).
+// Measured on GB300, order 4 / degree 12: the double-float kernel takes 116
+// registers unconstrained (4 CTAs per SM, 2.73M env/s) and 96 at 5 (2.97M);
+// FP32 and FP64 run best unconstrained (72 and 120-124 registers), which 7
+// and 4 reproduce.  An explicit 1 lets the allocator take 150-210 registers
+// and costs a third of the throughput.
 #ifndef EF_MIN_BLOCKS
 #define EF_MIN_BLOCKS 0
 #endif
@@ -224,12 +227,13 @@ template <typename T> __device__ __forceinline__ cpx<T> shfl_down_c(cpx<T> v, in
 // (G+1) rows of real parts followed by (G+1) rows of imaginary parts; the
 // output is Re(sum_k c_k AA_k) (the Cartesian components of an
 // EuclideanVector model).
+template <typename TE, int K> constexpr int ef_min_blocks() {
+  return EF_MIN_BLOCKS > 0 ? EF_MIN_BLOCKS
+         : K <= 4 ? (std::is_same<TE, df>::value ? 5 : std::is_same<TE, double>::value ? 4 : 7)
+                  : (std::is_same<TE, df>::value ? 4 : std::is_same<TE, double>::value ? 3 : 5);
+}
 template <typename TE, typename TG, int K, int NT, bool GRAD, bool ITEMS, bool CPX = false>
-#if EF_MIN_BLOCKS > 0
-__global__ void __launch_bounds__(NT, EF_MIN_BLOCKS) ef_kernel(EFArgs a) {
-#else
-__global__ void __launch_bounds__(NT) ef_kernel(EFArgs a) {
-#endif
+__global__ void __launch_bounds__(NT, ef_min_blocks<TE, CPX ? K + 1 : K>()) ef_kernel(EFArgs a) {
   static_assert(ITEMS || !CPX, "complex coefficients need the item schedule");
   constexpr bool SAME = std::is_same<TE, TG>::value;
   extern __shared__ __align__(16) unsigned char sm[];
@@ -357,11 +361,33 @@ __global__ void __launch_bounds__(NT) ef_kernel(EFArgs a) {
       const cpx<TG> gone = {TG(1), TG(0)};
       const TE ze = Arith<TE>::zero();
 #if EF_ITEM_RUNS
-      // prefix adjoints of this thread's run: target and running sum per depth
-      int rcur[KP];
-      cpx<TG> racc[KP];
+      // reverse-mode accumulation along this thread's run of items (sorted
+      // by prefix): the open path cur[0..cP) of the prefix trie with, per
+      // depth d, A at that node (acur), the product Q[d] = A_cur[0] ..
+      // A_cur[d] and the node's adjoint W[d] = dE/dQ[d].  A node closes when
+      // the path leaves it: D[cur[d]] += W[d] Q[d-1] and W[d-1] += W[d] acur[d]
+      // (the same sums as the per-item products over the other prefix
+      // members, src/pibasis.jl:397-432, grouped by trie node)
+      int cur[KP], cP = 0;
+      cpx<TG> W[KP], Q[KP], acur[KP];
 #pragma unroll
-      for (int d = 0; d < KP; ++d) { rcur[d] = -1; racc[d] = {TG(0), TG(0)}; }
+      for (int d = 0; d < KP; ++d) { cur[d] = -1; W[d] = {TG(0), TG(0)}; Q[d] = gone; acur[d] = gone; }
+      auto close_to = [&](int c) __attribute__((always_inline)) {
+#pragma unroll
+        for (int d = KP - 1; d >= 0; --d) {
+          const bool cl = d >= c && d < cP;
+          const int dm = d > 0 ? d - 1 : 0;
+          const cpx<TG> w = W[d];
+          if (cl) dacc(cur[d], d > 0 ? cmul(w, Q[dm]) : w);
+          if (d > 0) {
+            const cpx<TG> t = cmul(w, acur[d]);
+            W[dm].re += cl ? t.re : TG(0);
+            W[dm].im += cl ? t.im : TG(0);
+          }
+          W[d].re = cl ? TG(0) : w.re;
+          W[d].im = cl ? TG(0) : w.im;
+        }
+      };
 #endif
       for (int64_t f0 = tid; f0 < a.in; f0 += (int64_t)IU * NT) {
         int P[IU], nl[IU], vi[IU][KP], ul[IU][ITEM_G];
@@ -387,7 +413,8 @@ __global__ void __launch_bounds__(NT) ef_kernel(EFArgs a) {
             if (d < P[u]) {
               const cpx<TE> ae = AE[vi[u][d]];
               bar[u] = (d == 0) ? ae : cmul(bar[u], ae);
-              if (GRAD) aG[u][d] = AG[vi[u][d]];
+              // the adjoint's copy of A (AG = lower(AE)) from the value in registers
+              if (GRAD) aG[u][d] = {lower<TG>(ae.re), lower<TG>(ae.im)};
             }
           }
           H[u] = {ok ? load_coef<TE>(a.ic, f) : ze, (CPX && ok) ? load_coef<TE>(a.ic, (int64_t)(ITEM_G + 1) * a.in + f) : ze};
@@ -406,6 +433,45 @@ __global__ void __launch_bounds__(NT) ef_kernel(EFArgs a) {
         for (int u = 0; u < IU; ++u)
           if (P[u] > 0) eacc = eacc + re_mul<TE>(bar[u], H[u]);
         if (GRAD) {
+#if EF_ITEM_RUNS
+#pragma unroll
+          for (int u = 0; u < IU; ++u) {
+            if (P[u] > 0) {
+              const cpx<TG> h = {lower<TG>(H[u].re), lower<TG>(H[u].im)};
+              // depth of the first difference between the item's prefix and the path
+              int c = 0;
+#pragma unroll
+              for (int d = 0; d < KP; ++d)
+                if (c == d && d < P[u] && d < cP && vi[u][d] == cur[d]) c = d + 1;
+              close_to(c);
+              // extend the path by the item's prefix below depth c
+#pragma unroll
+              for (int d = 0; d < KP; ++d) {
+                const bool ext = d >= c && d < P[u];
+                const cpx<TG> q = d > 0 ? cmul(Q[d > 0 ? d - 1 : 0], aG[u][d]) : aG[u][d];
+                cur[d] = ext ? vi[u][d] : cur[d];
+                acur[d] = ext ? aG[u][d] : acur[d];
+                Q[d] = ext ? q : Q[d];
+              }
+              cP = P[u];
+#pragma unroll
+              for (int d = 0; d < KP; ++d) {
+                // selects, not a branch: keeps W in registers
+                const bool leaf = d == cP - 1;
+                W[d].re += leaf ? h.re : TG(0);
+                W[d].im += leaf ? h.im : TG(0);
+              }
+              // only full-length prefixes carry leaves
+              const cpx<TG> bG = Q[KP - 1];
+#pragma unroll
+              for (int g = 0; g < ITEM_G; ++g)
+                if (g < nl[u]) {
+                  if constexpr (CPX) dacc(ul[u][g], cmul(bG, cpx<TG>{lower<TG>(cl[u][g]), lower<TG>(cli[u][g])}));
+                  else dacc(ul[u][g], cscale(bG, lower<TG>(cl[u][g])));
+                }
+            }
+          }
+#else
           cpx<TG> v[IU][KP];
 #pragma unroll
           for (int u = 0; u < IU; ++u) {
@@ -431,23 +497,6 @@ __global__ void __launch_bounds__(NT) ef_kernel(EFArgs a) {
                 else dacc(ul[u][g], cscale(bG, lower<TG>(cl[u][g])));
               }
           }
-#if EF_ITEM_RUNS
-#pragma unroll
-          for (int u = 0; u < IU; ++u)
-#pragma unroll
-            for (int d = 0; d < KP; ++d) {
-              if (d < P[u]) {
-                if (vi[u][d] != rcur[d]) {
-                  if (rcur[d] >= 0) dacc(rcur[d], racc[d]);
-                  rcur[d] = vi[u][d];
-                  racc[d] = v[u][d];
-                } else {
-                  racc[d].re += v[u][d].re;
-                  racc[d].im += v[u][d].im;
-                }
-              }
-            }
-#else
 #pragma unroll
           for (int d = 0; d < KP; ++d) {
             if (d < KP - 1) {
@@ -478,11 +527,7 @@ __global__ void __launch_bounds__(NT) ef_kernel(EFArgs a) {
         }
       }
 #if EF_ITEM_RUNS
-      if (GRAD) {
-#pragma unroll
-        for (int d = 0; d < KP; ++d)
-          if (rcur[d] >= 0) dacc(rcur[d], racc[d]);
-      }
+      if (GRAD) close_to(0);
 #endif
     }
     const double esum = block_sum(lower<double>(eacc), red);

@@ -83,12 +83,21 @@ int main(int argc, char **argv) {
   std::vector<C> Di(nA);
   const int KP = it.KP, G = ITEM_G;
 #if EF_ITEM_RUNS
-  // per-thread contiguous runs (slot = j * NT + thread), prefix adjoints
-  // accumulated per depth and flushed when the target changes, as the kernel
+  // per-thread contiguous runs (slot = j * NT + thread) with reverse-mode
+  // accumulation along the open prefix path, as the kernel: node adjoints
+  // W[d], products Q[d] = A_cur[0] .. A_cur[d]; a node closes when the path
+  // leaves it (D[cur[d]] += W[d] Q[d-1], W[d-1] += W[d] A_cur[d])
   for (int t = 0; t < NT; ++t) {
-    int cur[8];
-    C acc[8];
-    for (int e = 0; e < 8; ++e) { cur[e] = -1; acc[e] = 0; }
+    int cur[8], cP = 0;
+    C Wn[8], Q[8];
+    for (int e = 0; e < 8; ++e) { cur[e] = -1; Wn[e] = 0; Q[e] = 1; }
+    auto close_to = [&](int c) {
+      for (int d = cP - 1; d >= c; --d) {
+        Di[cur[d]] += d > 0 ? Wn[d] * Q[d - 1] : Wn[d];
+        if (d > 0) Wn[d - 1] += Wn[d] * A[cur[d]];
+        Wn[d] = 0;
+      }
+    };
     for (int64_t f = t; f < it.n; f += NT) {
       const uint16_t *r = &it.rec[8 * f];
       const uint8_t *b = (const uint8_t *)r;
@@ -98,25 +107,22 @@ int main(int argc, char **argv) {
         uint8_t w = g == 0 ? it.wown[f] : it.wleaf[f * G + g - 1];
         return k < 0 ? 0.0 : w * ct[k];
       };
+      if (P == 0) continue;
       C bar = 1;
       for (int e = 0; e < P; ++e) bar *= A[r[e]];
       C H = coef(0);
       for (int g = 0; g < nl; ++g) H += coef(g + 1) * A[r[5 + g]];
-      if (P > 0) Ei += (bar * H).real();
-      for (int g = 0; g < nl; ++g) Di[r[5 + g]] += coef(g + 1) * bar;
-      for (int e = 0; e < P; ++e) {
-        C q = H;
-        for (int x = 0; x < P; ++x) if (x != e) q *= A[r[x]];
-        if (r[e] != cur[e]) {
-          if (cur[e] >= 0) Di[cur[e]] += acc[e];
-          cur[e] = r[e];
-          acc[e] = q;
-        } else {
-          acc[e] += q;
-        }
-      }
+      Ei += (bar * H).real();
+      int c = 0;
+      while (c < P && c < cP && r[c] == cur[c]) ++c;
+      close_to(c);
+      for (int d = c; d < P; ++d) { cur[d] = r[d]; Q[d] = (d > 0 ? Q[d - 1] : C(1)) * A[r[d]]; }
+      cP = P;
+      Wn[P - 1] += H;
+      if (nl > 0 && P != KP) { printf("leaves-on-short-prefix\n"); return 1; }
+      for (int g = 0; g < nl; ++g) Di[r[5 + g]] += coef(g + 1) * Q[KP - 1];
     }
-    for (int e = 0; e < KP; ++e) if (cur[e] >= 0) Di[cur[e]] += acc[e];
+    close_to(0);
   }
 #else
   // 32 consecutive items per warp, segmented by head bits
