@@ -367,7 +367,7 @@ __global__ void __launch_bounds__(NT, ef_min_blocks<TE, CPX ? K + 1 : K>()) ef_k
       // A_cur[d] and the node's adjoint W[d] = dE/dQ[d].  A node closes when
       // the path leaves it: D[cur[d]] += W[d] Q[d-1] and W[d-1] += W[d] acur[d]
       // (the same sums as the per-item products over the other prefix
-      // members, src/pibasis.jl:397-432, grouped by trie node)
+      // members, src/pibasis.jl:338-390, grouped by trie node)
       int cur[KP], cP = 0;
       cpx<TG> W[KP], Q[KP], acur[KP];
 #pragma unroll

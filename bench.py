@@ -478,9 +478,13 @@ def main():
         return {"E_rel_max_vs_fp64": float(np.max(np.abs(E - E64) / scale)),
                 "F_rel_max_vs_fp64": float(np.max(np.abs(G - G64)) / np.max(np.abs(G64))),
                 "envs_compared": n64}
-    # plain FP32 (fast, not within the 1e-6 bar)
+    # plain FP32 (fast, not within the 1e-6 bar), launch configuration tuned
+    # on the first 20,000 environments
     ctx32 = Context(spec, "fp32", device=local)
     ctx32.set_params(c)
+    nt = min(nenv, 20_000)
+    ctx32.autotune(off_d[:nt + 1], rr_d, sp_d, E_d[:nt], G_d, reps=1, stream=stream.cuda_stream)
+    torch.cuda.synchronize()
     t32p, _ = timed(ctx32, args.steps, args.warmup)
     err32 = errors()
     # the chosen form: double-float energy path, FP32 adjoint and forces,
