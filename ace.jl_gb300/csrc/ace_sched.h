@@ -184,19 +184,21 @@ inline Interleaved interleave(const Schedule &s, int nthreads) {
 // coefficient of the prefix function itself, if p is a function, rides on
 // the prefix's first item.  Functions of order < K-1 are items with no
 // leaves.  Items are sorted lexicographically by prefix (full-length prefixes
-// first), so items sharing a prefix (v1..vd) are adjacent; a warp processes
+// first), so items sharing a prefix (v1..vd) are adjacent.  With the default
+// layout (EF_ITEM_RUNS = 1) each thread takes a contiguous run of the sorted
+// items and accumulates the prefix adjoints in reverse mode along the run
+// (per trie node of its open path); with EF_ITEM_RUNS = 0 a warp processes
 // 32 consecutive items and reduces the adjoint contributions to shared
-// targets with segmented shuffles.  `head` bit d marks the first item of a
-// run of equal (v1..v_{d+1}) within its warp.
+// targets with segmented shuffles, for which `head` bit d marks the first
+// item of a run of equal (v1..v_{d+1}) within its warp.
 //
 // Record (16 bytes): idx[0..4] prefix (uint16), idx[5..6] leaves, byte 14 =
 // P | nleaf << 4, byte 15 = head bits.  P == 0 marks padding.
 static constexpr int ITEM_G = 2;
 
-// item layout: 1 (default) = per-thread contiguous runs with
-// register-accumulated prefix adjoints (measured on GB300: FP64 +13-26 %,
-// fp32x2 unchanged); 0 = uniform stride with warp-segmented prefix
-// reductions using the head bits
+// item layout: 1 (default) = per-thread contiguous runs with the prefix
+// adjoints accumulated in registers along the run; 0 = uniform stride with
+// warp-segmented prefix reductions using the head bits
 #ifndef EF_ITEM_RUNS
 #define EF_ITEM_RUNS 1
 #endif

@@ -173,14 +173,9 @@ def measured_peaks(torch):
     return out
 
 
-def cpu_baseline(spec, c, b, threads=0, target_s=8.0):
-    """The oracle (FP64 CPU restatement of the reference evaluator) on a
-    bounded sample of the same workload, all host threads."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle
-    oracle.build()
-    orc = oracle.Oracle(spec, c)
-    nthreads = threads or os.cpu_count()
+def _time_oracle(orc, b, nthreads, target_s):
+    """(environments, seconds) of the oracle's E+F on the first n environments,
+    n grown until one call takes target_s or covers the batch."""
     n = 256
     while True:
         off = b.offsets[:n + 1]
@@ -189,10 +184,25 @@ def cpu_baseline(spec, c, b, threads=0, target_s=8.0):
         orc.energy_forces(off, b.rr[:off[-1]], sp, nthreads=nthreads)
         dt = time.perf_counter() - t0
         if dt >= target_s or n >= b.nenv:
-            break
+            return n, dt
         n = min(b.nenv, int(n * max(2.0, 1.2 * target_s / max(dt, 1e-3))))
+
+
+def cpu_baseline(spec, c, b, threads=0, target_s=8.0):
+    """The oracle (FP64 CPU restatement of the reference evaluator) on a
+    bounded sample of the same workload: all host threads (the reported
+    value) and one thread (``single_thread``)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    orc = oracle.Oracle(spec, c)
+    nthreads = threads or os.cpu_count()
+    n, dt = _time_oracle(orc, b, nthreads, target_s)
+    n1, dt1 = _time_oracle(orc, b, 1, target_s / 2)
     return {"value": n / dt, "unit": UNIT, "cores": nthreads, "kind": "port",
-            "sample": f"first {n} environments of the workload, E+F, FP64, {nthreads} threads, {dt:.1f} s"}
+            "sample": f"first {n} environments of the workload, E+F, FP64, {nthreads} threads, {dt:.1f} s",
+            "single_thread": {"value": n1 / dt1, "unit": UNIT,
+                              "sample": f"first {n1} environments, 1 thread, {dt1:.1f} s"}}
 
 
 def run_reference(args):
