@@ -80,3 +80,21 @@ def test_rpe_basis_symmetric_and_invariant():
     for sig in stab:
         idx = [keys[tuple(r[t] for t in sig)] for r in mm.tolist()]
         assert np.allclose(U[:, idx], U, atol=1e-12)
+
+
+@pytest.mark.parametrize("N,pcut,pin,Nquad", [(8, 2, 0, None), (16, 2, 0, None), (12, 2, 2, 500), (6, 0, 0, 300)])
+def test_radial_polynomials_orthonormal_on_their_grid(N, pcut, pin, Nquad):
+    # The discrete Stieltjes procedure (src/polynomials/orthpolys.jl:153-218)
+    # makes P_1..P_N orthonormal in the weighted discrete inner product on
+    # the grid it was built on; the reference's own test asks for this check
+    # (test/polynomials/test_orthpolys.jl: "replace this test with an
+    # orthogonality test").
+    from ace_gb300.radial import PolyTransform, discrete_jacobi
+    J = discrete_jacobi(N, pcut=pcut, xcut=5.0, pin=pin, xin=0.8, Nquad=Nquad, trans=PolyTransform(2, 1.0))
+    P = J.evaluate(J.tdf)
+    G = P.T @ (J.ww[:, None] * P)
+    assert np.max(np.abs(G - np.eye(N))) < 1e-10
+    # the envelope vanishes at the cutoff end of the transformed interval
+    tc = J.tl if J.pl > 0 else J.tr
+    if pcut > 0:
+        assert np.max(np.abs(J.evaluate(np.array([tc])))) < 1e-14
