@@ -74,8 +74,14 @@ def init1pspec(nR: int, maxL: int, maxdeg: float, nspecies: int = 1) -> OnePSpec
     return OnePSpec(mu[p], n[p], l[p], m[p])
 
 
+# partial tuples expanded per step of the enumeration: bounds its memory
+# (rows of k indices and three sums) independently of the basis size
+_ENUM_ROWS = 1 << 22
+
+
 def gensparse_ordered(deg: np.ndarray, ls: np.ndarray, ms: np.ndarray,
-                      maxorder: int, maxdeg: float, prop: str = "invariant") -> list:
+                      maxorder: int, maxdeg: float, prop: str = "invariant",
+                      chunk_rows: int = _ENUM_ROWS) -> list:
     """All ascending tuples v_1 <= ... <= v_k (0-based A indices, k = 0..maxorder)
     with sum(deg[v]) <= maxdeg, kept when k <= 1 or (sum l even and sum m == 0)
     for the Invariant property (src/properties.jl:133-150), or when sum l is
@@ -83,53 +89,80 @@ def gensparse_ordered(deg: np.ndarray, ls: np.ndarray, ms: np.ndarray,
     (src/properties.jl:189-203,240-246).
     Returned per order k as int arrays (N_k, k), each in lexicographic order,
     which is gensparse's enumeration order (order-major because shorter
-    tuples are padded with leading zeros)."""
+    tuples are padded with leading zeros).
+
+    The enumeration extends partial tuples one index at a time; a set of
+    prefixes whose extension would exceed ``chunk_rows`` rows is split in two
+    (in order) and each half is enumerated to the end and filtered before
+    the next, so memory stays bounded while the output order is unchanged."""
     deg = np.asarray(deg)
     assert np.all(np.diff(deg) >= 0), "A spec must be sorted by degree"
-    nA = len(deg)
+    ls = np.asarray(ls, dtype=np.int64)
+    ms = np.asarray(ms, dtype=np.int64)
     vec = prop == "vector"
     sphL = prop[1] if isinstance(prop, tuple) and prop[0] == "spherical" else None
     mslack = 1 if vec else (sphL if sphL is not None else 0)
     const = not vec and (sphL is None or sphL == 0)
+
+    def final_filter(tup, msum, lsum, k):
+        if not len(tup):
+            return tup
+        if vec:
+            return tup[(lsum % 2 == 1) & (np.abs(msum) <= 1)]
+        if sphL is not None:
+            if k >= 2 or sphL > 0:
+                return tup[(lsum % 2 == sphL % 2) & (np.abs(msum) <= sphL)]
+            return tup
+        if k >= 2:
+            return tup[(lsum % 2 == 0) & (msum == 0)]
+        return tup
+
+    def extend(tup, dsum, msum, lsum, t, k, parts):
+        """Enumerate the completions of the prefixes `tup` (t indices each)
+        to order k; append the filtered tuples to `parts` in order."""
+        if t == k:
+            f = final_filter(tup, msum, lsum, k)
+            if len(f):
+                parts.append(f)
+            return
+        rem = k - t
+        lo = tup[:, -1] if t > 0 else np.zeros(len(tup), dtype=np.int64)
+        # remaining rem entries all have degree >= deg[v]
+        hi = np.searchsorted(deg, (maxdeg - dsum) / rem, side="right")
+        cnt = np.maximum(hi - lo, 0)
+        total = int(cnt.sum())
+        if total == 0:
+            return
+        if total > chunk_rows and len(tup) > 1:
+            h = len(tup) // 2
+            extend(tup[:h], dsum[:h], msum[:h], lsum[:h], t, k, parts)
+            extend(tup[h:], dsum[h:], msum[h:], lsum[h:], t, k, parts)
+            return
+        rows = np.repeat(np.arange(len(tup)), cnt)
+        starts = np.repeat(lo - np.cumsum(np.concatenate([[0], cnt[:-1]])), cnt)
+        v = np.arange(total) + starts
+        tup2 = np.concatenate([tup[rows], v[:, None]], axis=1)
+        dsum2 = dsum[rows] + deg[v]
+        msum2 = msum[rows] + ms[v]
+        lsum2 = lsum[rows] + ls[v]
+        keep = dsum2 <= maxdeg + 1e-12
+        if t < k - 1:
+            # prune: the remaining entries have |m| <= l <= deg <= maxdeg - dsum
+            keep &= np.abs(msum2) <= (maxdeg - dsum2) + mslack + 1e-12
+        del rows, starts, v
+        extend(tup2[keep], dsum2[keep], msum2[keep], lsum2[keep], t + 1, k, parts)
+
     out = [np.zeros((1 if const else 0, 0), dtype=np.int64)]  # order 0: the constant (L = 0 outputs only)
     for k in range(1, maxorder + 1):
-        # rows: partial tuples, their degree sum and m sum
-        tup = np.zeros((1, 0), dtype=np.int64)
-        dsum = np.zeros(1)
-        msum = np.zeros(1, dtype=np.int64)
-        lsum = np.zeros(1, dtype=np.int64)
-        for t in range(k):
-            rem = k - t
-            lo = tup[:, -1] if t > 0 else np.zeros(len(tup), dtype=np.int64)
-            # remaining rem entries all have degree >= deg[v]
-            hi = np.searchsorted(deg, (maxdeg - dsum) / rem, side="right")
-            cnt = np.maximum(hi - lo, 0)
-            if cnt.sum() == 0:
-                tup = np.zeros((0, t + 1), dtype=np.int64)
-                break
-            rows = np.repeat(np.arange(len(tup)), cnt)
-            starts = np.repeat(lo - np.cumsum(np.concatenate([[0], cnt[:-1]])), cnt)
-            v = np.arange(cnt.sum()) + starts
-            tup = np.concatenate([tup[rows], v[:, None]], axis=1)
-            dsum = dsum[rows] + deg[v]
-            msum = msum[rows] + ms[v]
-            lsum = lsum[rows] + ls[v]
-            keep = dsum <= maxdeg + 1e-12
-            if t < k - 1:
-                # prune: the remaining entries have |m| <= l <= deg <= maxdeg - dsum
-                keep &= np.abs(msum) <= (maxdeg - dsum) + mslack + 1e-12
-            tup, dsum, msum, lsum = tup[keep], dsum[keep], msum[keep], lsum[keep]
-        if vec and len(tup):
-            tup = tup[(lsum % 2 == 1) & (np.abs(msum) <= 1)]
-        elif sphL is not None and len(tup):
-            if k >= 2 or sphL > 0:
-                tup = tup[(lsum % 2 == sphL % 2) & (np.abs(msum) <= sphL)]
-        elif k >= 2 and len(tup):
-            keep = (lsum % 2 == 0) & (msum == 0)
-            tup = tup[keep]
-        if len(tup):
+        parts = []
+        extend(np.zeros((1, 0), dtype=np.int64), np.zeros(1), np.zeros(1, dtype=np.int64),
+               np.zeros(1, dtype=np.int64), 0, k, parts)
+        tup = np.concatenate(parts, axis=0) if parts else np.zeros((0, k), dtype=np.int64)
+        if len(tup) > 1:
+            # generated in lexicographic order already; keep the guarantee explicit
             order = np.lexsort(tup.T[::-1])
-            tup = tup[order]
+            if np.any(order != np.arange(len(tup))):
+                tup = tup[order]
         out.append(tup)
     return out
 

@@ -98,3 +98,17 @@ def test_radial_polynomials_orthonormal_on_their_grid(N, pcut, pin, Nquad):
     tc = J.tl if J.pl > 0 else J.tr
     if pcut > 0:
         assert np.max(np.abs(J.evaluate(np.array([tc])))) < 1e-14
+
+
+@pytest.mark.parametrize("deg,nspecies,order,prop", [(8, 1, 4, "invariant"), (8, 2, 3, "invariant"),
+                                                     (8, 1, 5, "vector"), (7, 1, 4, ("spherical", 2))])
+def test_gensparse_bounded_enumeration_is_order_preserving(deg, nspecies, order, prop):
+    # splitting the prefix sets (small row budget) must give the same tuples
+    # in the same (lexicographic) order as one unsplit enumeration
+    from ace_gb300.spec import init1pspec
+    a = init1pspec(deg, deg, deg, nspecies)
+    full = gensparse_ordered(a.degree.astype(float), a.l, a.m, order, deg, prop, chunk_rows=1 << 30)
+    split = gensparse_ordered(a.degree.astype(float), a.l, a.m, order, deg, prop, chunk_rows=64)
+    assert len(full) == len(split)
+    for x, y in zip(full, split):
+        assert x.shape == y.shape and np.array_equal(x, y)
