@@ -47,3 +47,21 @@ def test_flops_per_env_counts_the_reference_terms():
     per_env = sum(n * (6 * (k - 1) + 2) + n * (18 * max(k - 2, 0) + 6 + 4 * k) for k, n in nby.items() if k > 0)
     assert f0 == per_env
     assert np.isclose(bench.flops_per_env(spec, 30) - f0, 30 * (f1 - f0))
+
+
+def test_reference_arm_under_two_ranks_prints_one_line():
+    # launched like the multi-GPU bench (torchrun, one rank per GPU): rank 0
+    # alone runs the CPU reference and prints; the other rank exits 0
+    import socket
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    r = subprocess.run([sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
+                        "--master-addr", "127.0.0.1", "--master-port", str(port),
+                        os.path.join(ROOT, "bench.py"), "--impl", "reference", "--gpus", "2", "--steps", "1",
+                        "--warmup", "0"], capture_output=True, text=True, timeout=900, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [x for x in r.stdout.splitlines() if x.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
