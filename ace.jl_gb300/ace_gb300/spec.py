@@ -217,6 +217,165 @@ def _encode(rows: np.ndarray, base: int) -> np.ndarray:
     return k
 
 
+def _coupling_rows_loop(aspec, iAA2iA, orders, skeys, korder, aidx, base, maxorder, maxL, zero_tol):
+    """U rows of every class, one reference function (all m == 0) at a time in
+    AA order (src/symmbasis.jl:89-162): the class's rpe_basis over mrange(ll),
+    columns collapsed onto the ordered AA functions (_get_ordered), small
+    entries dropped.  The reference implementation of _coupling_rows."""
+    a_m = aspec.m
+    refmask = np.all(np.where(iAA2iA >= 0, a_m[np.maximum(iAA2iA, 0)] == 0, True), axis=1)
+    adeg = aspec.degree
+    Irow, Jcol, vals, Bdeg, Bclass = [], [], [], [], []
+    nB = 0
+    nclass = 0
+    for iAA in np.nonzero(refmask)[0]:
+        k = int(orders[iAA])
+        vs = iAA2iA[iAA, :k]
+        if k == 0:
+            Irow.append(np.array([nB])); Jcol.append(np.array([iAA])); vals.append(np.array([1.0]))
+            Bdeg.append(0.0); Bclass.append(nclass)
+            nB += 1; nclass += 1
+            continue
+        ll = tuple(int(x) for x in aspec.l[vs])
+        nn = tuple((int(a), int(b)) for a, b in zip(aspec.mu[vs], aspec.n[vs]))
+        U = rpe_basis(ll, _nn_pattern(nn))
+        if U.shape[0] == 0:
+            continue
+        mm = mrange(ll)
+        A = np.stack([aidx[aspec.mu[vs[t]], aspec.n[vs[t]], ll[t], mm[:, t] + maxL]
+                      for t in range(k)], axis=1)
+        assert np.all(A >= 0)
+        A = -np.sort(-A, axis=1)                       # _get_ordered
+        r = -np.ones((len(A), maxorder), dtype=np.int64)
+        r[:, :k] = A
+        pk = _encode(r, base)
+        pos = np.searchsorted(skeys, pk)
+        if np.any(pos >= len(skeys)) or np.any(skeys[np.minimum(pos, len(skeys) - 1)] != pk):
+            raise RuntimeError("bcol_ordered not in AA-spec")
+        cols = korder[pos]
+        ucols, inv = np.unique(cols, return_inverse=True)
+        Uc = np.zeros((U.shape[0], len(ucols)))
+        np.add.at(Uc.T, inv, U.T)
+        rmax = np.abs(Uc).max(axis=1, keepdims=True)
+        Uc[np.abs(Uc) <= zero_tol * rmax] = 0.0
+        d = float(sum(adeg[vs]))
+        for irow in range(U.shape[0]):
+            nzm = Uc[irow] != 0
+            Irow.append(np.full(int(nzm.sum()), nB)); Jcol.append(ucols[nzm]); vals.append(Uc[irow, nzm])
+            Bdeg.append(d); Bclass.append(nclass)
+            nB += 1
+        nclass += 1
+    return Irow, Jcol, vals, Bdeg, Bclass, nB, nclass
+
+
+def _coupling_rows(aspec, iAA2iA, orders, skeys, korder, aidx, base, maxorder, maxL, zero_tol):
+    """The rows of _coupling_rows_loop, computed once per class signature.
+
+    A class's U depends only on ll and the equality pattern of its (mu, n)
+    (rpe_basis), and so does the partition of its m-tuples into AA functions
+    (two m-tuples collapse onto one ordered function iff they agree up to
+    permutations within equal (mu, n, l) entries).  So the column sums, the
+    dropped entries and the row count are computed once per signature and
+    every member only looks up its own AA columns; rows are placed at the
+    offsets the loop would give them (same values, same row order)."""
+    a_m = aspec.m
+    refmask = np.all(np.where(iAA2iA >= 0, a_m[np.maximum(iAA2iA, 0)] == 0, True), axis=1)
+    ref = np.nonzero(refmask)[0]
+    F = len(ref)
+    V = iAA2iA[ref]
+    ks = orders[ref].astype(np.int64)
+    valid = V >= 0
+    Vc = np.maximum(V, 0)
+    Ls = np.where(valid, aspec.l[Vc], -1).astype(np.int64)
+    MU = aspec.mu[Vc].astype(np.int64)
+    NN = aspec.n[Vc].astype(np.int64)
+    nnkey = np.where(valid, MU * (int(NN.max(initial=0)) + 1) + NN, -1)
+    # first-occurrence labels of (mu, n) along each row (_nn_pattern)
+    lab = np.full(V.shape, -1, dtype=np.int64)
+    nlab = np.zeros(F, dtype=np.int64)
+    for t in range(maxorder):
+        first = np.full(F, -1, dtype=np.int64)
+        for s_ in range(t - 1, -1, -1):
+            first = np.where(valid[:, t] & (nnkey[:, s_] == nnkey[:, t]), lab[:, s_], first)
+        new = valid[:, t] & (first < 0)
+        lab[:, t] = np.where(new, nlab, first)
+        nlab += new
+    sig = ks.copy()
+    for t in range(maxorder):
+        sig = sig * 512 + (Ls[:, t] + 1) * 8 + (lab[:, t] + 1)
+    usig, ginv = np.unique(sig, return_inverse=True)
+    dsum = np.where(valid, aspec.degree[Vc], 0).sum(axis=1).astype(np.float64)
+
+    # per signature: U (rows), the m-tuples, and the collapse pattern
+    groups = []
+    nrows = np.zeros(F, dtype=np.int64)
+    for g in range(len(usig)):
+        mem = np.nonzero(ginv == g)[0]
+        f0 = mem[0]
+        k = int(ks[f0])
+        if k == 0:
+            groups.append((mem, None))
+            nrows[mem] = 1
+            continue
+        ll = tuple(int(x) for x in Ls[f0, :k])
+        pattern = tuple(int(x) for x in lab[f0, :k])
+        U = rpe_basis(ll, pattern)
+        if U.shape[0] == 0:
+            groups.append((mem, None))
+            continue
+        mm = mrange(ll)
+
+        def lookup(sub):
+            """AA index of every (member, m-tuple): (len(sub), len(mm))."""
+            A = np.stack([aidx[MU[sub, t][:, None], NN[sub, t][:, None], ll[t], (mm[:, t] + maxL)[None, :]]
+                          for t in range(k)], axis=2)
+            assert np.all(A >= 0)
+            A = -np.sort(-A, axis=2)                       # _get_ordered
+            r = -np.ones(A.shape[:2] + (maxorder,), dtype=np.int64)
+            r[:, :, :k] = A
+            pk = _encode(r.reshape(-1, maxorder), base)
+            pos = np.searchsorted(skeys, pk)
+            if np.any(pos >= len(skeys)) or np.any(skeys[np.minimum(pos, len(skeys) - 1)] != pk):
+                raise RuntimeError("bcol_ordered not in AA-spec")
+            return korder[pos].reshape(len(sub), -1)
+
+        # members in slices of ~2M (member, m-tuple) entries
+        step = max(1, (1 << 21) // max(1, len(mm)))
+        parts = []
+        for c0 in range(0, len(mem), step):
+            cols = lookup(mem[c0:c0 + step])
+            if c0 == 0:
+                _, first_idx, inv = np.unique(cols[0], return_index=True, return_inverse=True)
+                Uc = np.zeros((U.shape[0], len(first_idx)))
+                np.add.at(Uc.T, inv, U.T)
+                rmax = np.abs(Uc).max(axis=1, keepdims=True)
+                Uc[np.abs(Uc) <= zero_tol * rmax] = 0.0
+            parts.append(cols[:, first_idx])
+        groups.append((mem, (np.concatenate(parts, axis=0), Uc)))
+        nrows[mem] = U.shape[0]
+
+    off = np.concatenate([[0], np.cumsum(nrows)])
+    nB = int(off[-1])
+    has = nrows > 0
+    cls = np.cumsum(has) - 1                               # class index of each function with rows
+    nclass = int(has.sum())
+    Bdeg = np.repeat(dsum, nrows)
+    Bclass = np.repeat(cls, nrows)
+    Irow, Jcol, vals = [], [], []
+    for mem, data in groups:
+        if data is None:
+            if nrows[mem[0]] == 1:                         # the constant (order 0)
+                Irow.append(off[mem]); Jcol.append(ref[mem]); vals.append(np.ones(len(mem)))
+            continue
+        ccols, Uc = data
+        for irow in range(Uc.shape[0]):
+            nz = np.nonzero(Uc[irow])[0]
+            Irow.append(np.repeat(off[mem] + irow, len(nz)))
+            Jcol.append(ccols[:, nz].ravel())
+            vals.append(np.tile(Uc[irow, nz], len(mem)))
+    return Irow, Jcol, vals, list(Bdeg), list(Bclass), nB, nclass
+
+
 def symmetric_basis(maxorder: int, maxdeg: float, nR: int | None = None,
                     maxL: int | None = None, nspecies: int = 1,
                     r0: float = 1.0, rcut: float = 5.0, rin: float | None = None,
@@ -257,49 +416,10 @@ def symmetric_basis(maxorder: int, maxdeg: float, nR: int | None = None,
     aidx = -np.ones((nspecies, nR + 1, maxL + 1, 2 * maxL + 1), dtype=np.int64)
     aidx[aspec.mu, aspec.n, aspec.l, aspec.m + maxL] = np.arange(nA0)
 
-    # coupling: loop over reference functions (all m == 0)
-    a_m = aspec.m
-    refmask = np.all(np.where(iAA2iA >= 0, a_m[np.maximum(iAA2iA, 0)] == 0, True), axis=1)
-    Irow, Jcol, vals, Bdeg, Bclass = [], [], [], [], []
-    nB = 0
-    nclass = 0
-    for iAA in np.nonzero(refmask)[0]:
-        k = int(orders[iAA])
-        vs = iAA2iA[iAA, :k]
-        if k == 0:
-            Irow.append(np.array([nB])); Jcol.append(np.array([iAA])); vals.append(np.array([1.0]))
-            Bdeg.append(0.0); Bclass.append(nclass)
-            nB += 1; nclass += 1
-            continue
-        ll = tuple(int(x) for x in aspec.l[vs])
-        nn = tuple((int(a), int(b)) for a, b in zip(aspec.mu[vs], aspec.n[vs]))
-        U = rpe_basis(ll, _nn_pattern(nn))
-        if U.shape[0] == 0:
-            continue
-        mm = mrange(ll)
-        A = np.stack([aidx[aspec.mu[vs[t]], aspec.n[vs[t]], ll[t], mm[:, t] + maxL]
-                      for t in range(k)], axis=1)
-        assert np.all(A >= 0)
-        A = -np.sort(-A, axis=1)                       # _get_ordered
-        r = -np.ones((len(A), maxorder), dtype=np.int64)
-        r[:, :k] = A
-        pk = _encode(r, base)
-        pos = np.searchsorted(skeys, pk)
-        if np.any(pos >= len(skeys)) or np.any(skeys[np.minimum(pos, len(skeys) - 1)] != pk):
-            raise RuntimeError("bcol_ordered not in AA-spec")
-        cols = korder[pos]
-        ucols, inv = np.unique(cols, return_inverse=True)
-        Uc = np.zeros((U.shape[0], len(ucols)))
-        np.add.at(Uc.T, inv, U.T)
-        rmax = np.abs(Uc).max(axis=1, keepdims=True)
-        Uc[np.abs(Uc) <= zero_tol * rmax] = 0.0
-        d = float(sum(aspec.degree[vs]))
-        for irow in range(U.shape[0]):
-            nzm = Uc[irow] != 0
-            Irow.append(np.full(int(nzm.sum()), nB)); Jcol.append(ucols[nzm]); vals.append(Uc[irow, nzm])
-            Bdeg.append(d); Bclass.append(nclass)
-            nB += 1
-        nclass += 1
+    # coupling over the reference functions (all m == 0), grouped by class
+    # signature; row order as one loop over them (_coupling_rows_loop)
+    Irow, Jcol, vals, Bdeg, Bclass, nB, nclass = _coupling_rows(
+        aspec, iAA2iA, orders, skeys, korder, aidx, base, maxorder, maxL, zero_tol)
     Irow = np.concatenate(Irow); Jcol = np.concatenate(Jcol); vals = np.concatenate(vals)
     Ufull = sp.csr_matrix((vals, (Irow, Jcol)), shape=(nB, nAA0))
     Ufull.sum_duplicates()

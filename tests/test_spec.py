@@ -112,3 +112,17 @@ def test_gensparse_bounded_enumeration_is_order_preserving(deg, nspecies, order,
     assert len(full) == len(split)
     for x, y in zip(full, split):
         assert x.shape == y.shape and np.array_equal(x, y)
+
+
+@pytest.mark.parametrize("order,deg,nspecies", [(3, 8, 1), (4, 8, 2), (5, 8, 1), (2, 8, 4)])
+def test_grouped_coupling_matches_the_per_function_loop(order, deg, nspecies, monkeypatch):
+    # U, row degrees and class indices of the grouped construction are
+    # bit-identical to one loop over the reference functions
+    import ace_gb300.spec as S
+    grouped = S.symmetric_basis(order, deg, maxL=deg, nspecies=nspecies)
+    monkeypatch.setattr(S, "_coupling_rows", S._coupling_rows_loop)
+    loop = S.symmetric_basis(order, deg, maxL=deg, nspecies=nspecies)
+    for attr in ("indptr", "indices", "data"):
+        assert np.array_equal(getattr(grouped.U, attr), getattr(loop.U, attr))
+    assert np.array_equal(grouped.Bdeg, loop.Bdeg) and np.array_equal(grouped.Bclass, loop.Bclass)
+    assert np.array_equal(grouped.iAA2iA, loop.iAA2iA) and grouped.info == loop.info
