@@ -21,8 +21,10 @@
 #include <cmath>
 #include <cstdint>
 #include <map>
-#include <queue>
 #include <numeric>
+#include <queue>
+#include <tuple>
+#include <utility>
 #include <vector>
 
 namespace ace {
@@ -44,6 +46,25 @@ struct Schedule {
   std::vector<int8_t> msign;
 };
 
+// Lexicographic key of a descending index tuple of length <= 6: (v_j + 1) in
+// 16-bit fields from the most significant end and 0 past the tuple's end, so
+// keys order like std::vector comparison (a proper prefix sorts first).
+struct TupleKey {
+  uint64_t hi = 0, lo = 0;  // fields 0-1 in hi, 2-5 in lo
+  bool operator<(const TupleKey &o) const { return hi < o.hi || (hi == o.hi && lo < o.lo); }
+  bool operator==(const TupleKey &o) const { return hi == o.hi && lo == o.lo; }
+};
+
+inline TupleKey tuple_key(const int32_t *t, int o) {
+  TupleKey key;
+  for (int j = 0; j < 6; ++j) {
+    const uint64_t f = j < o ? (uint64_t)(uint16_t)(t[j] + 1) : 0u;
+    if (j < 2) key.hi = (key.hi << 16) | f;
+    else key.lo = (key.lo << 16) | f;
+  }
+  return key;
+}
+
 inline Schedule build_schedule(int nA, const int32_t *a_n, const int32_t *a_l, const int32_t *a_m,
                                const int32_t *a_mu, int64_t nAA, int K, const int32_t *orders,
                                const int32_t *iAA2iA, int64_t nB, const int64_t *U_indptr,
@@ -60,33 +81,59 @@ inline Schedule build_schedule(int nA, const int32_t *a_n, const int32_t *a_l, c
     if (it == aidx.end()) { ok = false; break; }
     partner[i] = it->second;
   }
-  // ---- partner AA functions
-  std::map<std::vector<int>, int64_t> tidx;
-  for (int64_t k = 0; k < nAA; ++k) {
-    std::vector<int> t(iAA2iA + k * K, iAA2iA + k * K + orders[k]);
-    tidx[t] = k;
-  }
+  // ---- partner AA functions: the keys of all tuples and of their partner
+  // tuples, both sorted, joined in one merge (for a repeated tuple the last
+  // function, as a map would give)
+  typedef std::pair<TupleKey, int64_t> KeyedK;
+  auto by_key = [](const KeyedK &a, const KeyedK &b) {
+    return a.first < b.first || (a.first == b.first && a.second < b.second);
+  };
+  std::vector<KeyedK> keyed((size_t)nAA);
+  for (int64_t k = 0; k < nAA; ++k) keyed[k] = {tuple_key(iAA2iA + k * K, orders[k]), k};
+  std::sort(keyed.begin(), keyed.end(), by_key);
   std::vector<int64_t> pk(nAA, -1);
   if (ok) {
-    for (int64_t k = 0; k < nAA && ok; ++k) {
-      std::vector<int> t;
-      for (int j = 0; j < orders[k]; ++j) t.push_back(partner[iAA2iA[k * K + j]]);
-      std::sort(t.begin(), t.end(), std::greater<int>());
-      auto it = tidx.find(t);
-      if (it == tidx.end()) { ok = false; break; }
-      pk[k] = it->second;
+    std::vector<KeyedK> pkeyed((size_t)nAA);
+    int32_t t[8];
+    for (int64_t k = 0; k < nAA; ++k) {
+      const int o = orders[k];
+      for (int j = 0; j < o; ++j) t[j] = partner[iAA2iA[k * K + j]];
+      std::sort(t, t + o, std::greater<int32_t>());
+      pkeyed[k] = {tuple_key(t, o), k};
+    }
+    std::sort(pkeyed.begin(), pkeyed.end(), by_key);
+    size_t a = 0;
+    for (size_t i = 0; i < pkeyed.size(); ++i) {
+      const TupleKey &key = pkeyed[i].first;
+      while (a < keyed.size() && keyed[a].first < key) ++a;
+      size_t e = a;
+      while (e < keyed.size() && keyed[e].first == key) ++e;
+      if (e == a) { ok = false; break; }
+      pk[pkeyed[i].second] = keyed[e - 1].second;
     }
   }
-  // ---- U columns of partners must agree (then c~ agrees for every c)
+  std::vector<std::pair<TupleKey, int64_t>>().swap(keyed);
+  // ---- U columns of partners must agree (then c~ agrees for every c):
+  // columns of U (CSC, rows ascending) by counting sort
   if (ok && nB > 0) {
-    std::vector<std::vector<std::pair<int64_t, double>>> cols(nAA);
+    const int64_t nnz = U_indptr[nB];
+    std::vector<int64_t> cptr(nAA + 1, 0);
+    for (int64_t j = 0; j < nnz; ++j) cptr[U_indices[j] + 1]++;
+    for (int64_t k = 0; k < nAA; ++k) cptr[k + 1] += cptr[k];
+    std::vector<int64_t> crow(nnz), fill(cptr.begin(), cptr.end() - 1);
+    std::vector<double> cval(nnz);
     for (int64_t b = 0; b < nB; ++b)
-      for (int64_t j = U_indptr[b]; j < U_indptr[b + 1]; ++j) cols[U_indices[j]].push_back({b, U_data[j]});
+      for (int64_t j = U_indptr[b]; j < U_indptr[b + 1]; ++j) {
+        const int64_t q = fill[U_indices[j]]++;
+        crow[q] = b;
+        cval[q] = U_data[j];
+      }
     for (int64_t k = 0; k < nAA && ok; ++k) {
-      const auto &a = cols[k], &b = cols[pk[k]];
-      if (a.size() != b.size()) { ok = false; break; }
-      for (size_t j = 0; j < a.size(); ++j)
-        if (a[j].first != b[j].first || std::fabs(a[j].second - b[j].second) > 1e-12 * (1.0 + std::fabs(a[j].second))) {
+      const int64_t a0 = cptr[k], na = cptr[k + 1] - a0, b0 = cptr[pk[k]], nb = cptr[pk[k] + 1] - b0;
+      if (na != nb) { ok = false; break; }
+      for (int64_t j = 0; j < na; ++j)
+        if (crow[a0 + j] != crow[b0 + j] ||
+            std::fabs(cval[a0 + j] - cval[b0 + j]) > 1e-12 * (1.0 + std::fabs(cval[a0 + j]))) {
           ok = false; break;
         }
     }
@@ -114,29 +161,31 @@ inline Schedule build_schedule(int nA, const int32_t *a_n, const int32_t *a_l, c
     }
   }
   // ---- lexicographic order of the descending tuples (prefix first)
-  std::vector<size_t> perm(keep.size());
-  std::iota(perm.begin(), perm.end(), 0);
-  auto tup = [&](size_t i) { const int64_t k = keep[i]; return std::vector<int>(iAA2iA + k * K, iAA2iA + k * K + orders[k]); };
-  std::vector<std::vector<int>> tuples(keep.size());
-  for (size_t i = 0; i < keep.size(); ++i) tuples[i] = tup(i);
-  std::stable_sort(perm.begin(), perm.end(), [&](size_t a, size_t b) { return tuples[a] < tuples[b]; });
+  std::vector<std::pair<TupleKey, size_t>> order(keep.size());
+  for (size_t i = 0; i < keep.size(); ++i) order[i] = {tuple_key(iAA2iA + keep[i] * K, orders[keep[i]]), i};
+  std::stable_sort(order.begin(), order.end(), [](const std::pair<TupleKey, size_t> &a, const std::pair<TupleKey, size_t> &b) {
+    return a.first < b.first;
+  });
   s.n = (int64_t)keep.size();
   s.v.assign((size_t)K * s.n, 0);
   s.ord.resize(s.n); s.q.resize(s.n); s.k.resize(s.n); s.w.resize(s.n);
-  std::vector<double> cost(s.n);
+  const int32_t *prev = nullptr;
+  int prev_o = 0;
   for (int64_t i = 0; i < s.n; ++i) {
-    const auto &t = tuples[perm[i]];
-    s.ord[i] = (uint8_t)t.size();
-    s.k[i] = (int32_t)keep[perm[i]];
-    s.w[i] = wts[perm[i]];
-    for (size_t j = 0; j < t.size(); ++j) s.v[(size_t)j * s.n + i] = (uint16_t)t[j];
+    const size_t pi = order[i].second;
+    const int64_t k = keep[pi];
+    const int o = orders[k];
+    const int32_t *t = iAA2iA + k * K;
+    s.ord[i] = (uint8_t)o;
+    s.k[i] = (int32_t)k;
+    s.w[i] = wts[pi];
+    for (int j = 0; j < o; ++j) s.v[(size_t)j * s.n + i] = (uint16_t)t[j];
     int qq = 0;
-    if (i > 0) {
-      const auto &p = tuples[perm[i - 1]];
-      while (qq < (int)std::min(p.size(), t.size()) && p[qq] == t[qq]) ++qq;
-    }
+    if (prev)
+      while (qq < std::min(prev_o, o) && prev[qq] == t[qq]) ++qq;
     s.q[i] = (uint8_t)qq;
-    cost[i] = 1.0 + 2.0 * (double)(t.size() - qq);
+    prev = t;
+    prev_o = o;
   }
   // ---- contiguous ranges of (nearly) equal length, one per thread
   s.start.assign(nthreads + 1, 0);
@@ -165,8 +214,11 @@ inline Interleaved interleave(const Schedule &s, int nthreads) {
   r.len = mx;
   r.rec.assign((size_t)mx * nthreads * 8, 0);
   r.perm.assign((size_t)mx * nthreads, -1);
-  for (int t = 0; t < nthreads; ++t)
-    for (int64_t i = s.start[t], j = 0; i < s.start[t + 1]; ++i, ++j) {
+  // slot order (j outer): the writes are sequential
+  for (int64_t j = 0; j < mx; ++j)
+    for (int t = 0; t < nthreads; ++t) {
+      const int64_t i = s.start[t] + j;
+      if (i >= s.start[t + 1]) continue;
       const size_t slot = (size_t)j * nthreads + t;
       uint16_t *rc = &r.rec[8 * slot];
       for (int d = 0; d < s.K && d < 6; ++d) rc[d] = s.v[(size_t)d * s.n + i];
@@ -218,31 +270,65 @@ inline ItemSchedule build_items(const Schedule &s, int nthreads) {
   it.K = K;
   it.KP = K > 1 ? K - 1 : 1;
   const int KP = it.KP;
-  struct Item { std::vector<int> pre; int64_t kown = -1; uint8_t wown = 0; std::vector<std::pair<int, std::pair<int64_t, uint8_t>>> leaves; };
-  std::map<std::vector<int>, std::vector<Item>> groups;   // prefix -> items (main group, |prefix| == KP)
-  std::map<std::vector<int>, Item> shorts;
+  struct Item {
+    int P = 0, nl = 0;
+    int pre[6] = {0, 0, 0, 0, 0, 0};
+    int64_t kown = -1;
+    uint8_t wown = 0;
+    int leaf[ITEM_G] = {};
+    int64_t kleaf[ITEM_G] = {};
+    uint8_t wleaf[ITEM_G] = {};
+  };
+  // One pass over the functions in lexicographic order: the functions with a
+  // prefix p of length K-1 (p itself first, then its extensions) are
+  // adjacent, so each prefix's items are formed where its first function
+  // appears; shorter functions are collected in order and appended.
+  std::vector<Item> items, shorts;
+  int cur[6] = {0, 0, 0, 0, 0, 0};
+  bool have = false;
+  size_t cur_first = 0;
+  auto vat = [&](int64_t i, int j) { return (int)s.v[(size_t)j * s.n + i]; };
+  auto open_group = [&](int64_t i) {  // the group of prefix v[0..KP) of function i
+    bool same = have;
+    for (int j = 0; j < KP && same; ++j) same = cur[j] == vat(i, j);
+    if (!same) {
+      Item x;
+      x.P = KP;
+      for (int j = 0; j < KP; ++j) cur[j] = x.pre[j] = vat(i, j);
+      items.push_back(x);
+      cur_first = items.size() - 1;
+      have = true;
+    }
+  };
   for (int64_t i = 0; i < s.n; ++i) {
     const int o = s.ord[i];
-    std::vector<int> t(o);
-    for (int j = 0; j < o; ++j) t[j] = s.v[(size_t)j * s.n + i];
     if (K > 1 && o == K) {
-      std::vector<int> pre(t.begin(), t.end() - 1);
-      auto &g = groups[pre];
-      if (g.empty() || (int)g.back().leaves.size() == ITEM_G) { g.emplace_back(); g.back().pre = pre; }
-      g.back().leaves.push_back({t.back(), {s.k[i], s.w[i]}});
+      open_group(i);
+      if (items.back().nl == ITEM_G) {
+        Item x;
+        x.P = KP;
+        for (int j = 0; j < KP; ++j) x.pre[j] = cur[j];
+        items.push_back(x);
+      }
+      Item &b = items.back();
+      b.leaf[b.nl] = vat(i, K - 1);
+      b.kleaf[b.nl] = s.k[i];
+      b.wleaf[b.nl] = s.w[i];
+      ++b.nl;
     } else if (o == KP) {
-      auto &g = groups[t];
-      if (g.empty()) { g.emplace_back(); g.back().pre = t; }
-      g.front().kown = s.k[i];
-      g.front().wown = s.w[i];
+      open_group(i);
+      items[cur_first].kown = s.k[i];
+      items[cur_first].wown = s.w[i];
     } else {
-      Item x; x.pre = t; x.kown = s.k[i]; x.wown = s.w[i];
-      shorts[t] = x;
+      Item x;
+      x.P = o;
+      for (int j = 0; j < o; ++j) x.pre[j] = vat(i, j);
+      x.kown = s.k[i];
+      x.wown = s.w[i];
+      shorts.push_back(x);
     }
   }
-  std::vector<Item> items;
-  for (auto &kv : groups) for (auto &x : kv.second) items.push_back(x);
-  for (auto &kv : shorts) items.push_back(kv.second);
+  items.insert(items.end(), shorts.begin(), shorts.end());
   const int64_t n0 = (int64_t)items.size();
   it.n = ((n0 + nthreads - 1) / nthreads) * nthreads;
   if (it.n == 0) it.n = nthreads;
@@ -267,15 +353,15 @@ inline ItemSchedule build_items(const Schedule &s, int nthreads) {
   it.wleaf.assign((size_t)it.n * ITEM_G, 0);
   for (int64_t f = 0; f < nfill; ++f) {
     const Item &x = items[f];
-    if (x.pre.empty() && x.leaves.empty() && x.kown < 0) continue;  // padding
+    if (x.P == 0 && x.nl == 0 && x.kown < 0) continue;  // padding
     uint16_t *r = &it.rec[8 * f];
-    const int P = (int)x.pre.size();
+    const int P = x.P;
     for (int d = 0; d < P; ++d) r[d] = (uint16_t)x.pre[d];
-    const int nl = (int)x.leaves.size();
+    const int nl = x.nl;
     for (int g = 0; g < nl; ++g) {
-      ((uint16_t *)r)[5 + g] = (uint16_t)x.leaves[g].first;
-      it.kleaf[(size_t)f * ITEM_G + g] = x.leaves[g].second.first;
-      it.wleaf[(size_t)f * ITEM_G + g] = x.leaves[g].second.second;
+      ((uint16_t *)r)[5 + g] = (uint16_t)x.leaf[g];
+      it.kleaf[(size_t)f * ITEM_G + g] = x.kleaf[g];
+      it.wleaf[(size_t)f * ITEM_G + g] = x.wleaf[g];
     }
     it.kown[f] = x.kown;
     it.wown[f] = x.wown;
@@ -284,7 +370,7 @@ inline ItemSchedule build_items(const Schedule &s, int nthreads) {
       bool head = (f % 32 == 0);
       if (!head) {
         const Item &y = items[f - 1];
-        if ((int)y.pre.size() != P || d >= P) head = true;
+        if (y.P != P || d >= P) head = true;
         else for (int e = 0; e <= d; ++e) if (y.pre[e] != x.pre[e]) { head = true; break; }
       }
       if (head) heads |= (uint8_t)(1u << d);
