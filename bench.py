@@ -15,10 +15,13 @@ device->host copy of energies and gradients inside the timed region).
 (``learned_4sp`` distils and times the learned radial form on the 4-species
 model):
 ``ord5_deg16`` (order 5, degree 16, L 16; 500,000 environments x 30
-neighbours) and ``ord4_deg10_4sp`` (4 species, order 4, degree 10, L 10;
+neighbours), ``ord4_deg10_4sp`` (4 species, order 4, degree 10, L 10;
 250,000 environments whose neighbour counts are 60 % U{40..80} and 40 %
-U{8..20}, species uniform).  On those the FP64 form is timed on a prefix of
-the batch (``fp64_envs``) to keep a step within seconds.
+U{8..20}, species uniform) and ``ord4_deg14_4sp`` (the same at degree 14:
+24.8M AA functions; run it with few steps, e.g. ``--steps 2 --warmup 1``).
+On those the FP64 form is timed on a prefix of the batch (``fp64_envs``) to
+keep a step within seconds, and ``autotune_envs`` bounds the autotuner's
+batch.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--workload NAME]
 """
@@ -50,6 +53,9 @@ WORKLOADS = {
     "ord4_deg10_4sp": dict(name="ace-invariant 4 species ord4 deg10 L10, 250k envs, J 60% U{40..80} / 40% U{8..20}",
                            maxorder=4, maxdeg=10, maxL=10, nspecies=4, nenv=250_000, jlo=8, jhi=80, seed=2024,
                            bimodal=(0.6, (40, 80), (8, 20)), fp64_envs=20_000),
+    "ord4_deg14_4sp": dict(name="ace-invariant 4 species ord4 deg14 L14, 250k envs, J 60% U{40..80} / 40% U{8..20}",
+                           maxorder=4, maxdeg=14, maxL=14, nspecies=4, nenv=250_000, jlo=8, jhi=80, seed=2024,
+                           bimodal=(0.6, (40, 80), (8, 20)), fp64_envs=2_000, autotune_envs=5_000),
 }
 WORKLOAD = WORKLOADS["ord4_deg12"]
 
@@ -492,7 +498,7 @@ def main():
     # on the first 20,000 environments
     ctx32 = Context(spec, "fp32", device=local)
     ctx32.set_params(c)
-    nt = min(nenv, 20_000)
+    nt = min(nenv, 20_000, WORKLOAD.get("autotune_envs") or nenv)
     ctx32.autotune(off_d[:nt + 1], rr_d, sp_d, E_d[:nt], G_d, reps=1, stream=stream.cuda_stream)
     torch.cuda.synchronize()
     t32p, _ = timed(ctx32, args.steps, args.warmup)
@@ -501,7 +507,8 @@ def main():
     # launch configuration picked by the autotuner on this batch
     ctx = Context(spec, CHOSEN, device=local)
     ctx.set_params(c)
-    tuned = ctx.autotune(off_d, rr_d, sp_d, E_d, G_d, reps=1, stream=stream.cuda_stream)
+    na = min(nenv, WORKLOAD.get("autotune_envs") or nenv)
+    tuned = ctx.autotune(off_d[:na + 1], rr_d, sp_d, E_d[:na], G_d, reps=1, stream=stream.cuda_stream)
     torch.cuda.synchronize()
     with Clocks(local) as clk:
         t32, launches = timed(ctx, args.steps, args.warmup)
