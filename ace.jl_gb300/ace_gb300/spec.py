@@ -117,6 +117,49 @@ def gensparse_ordered(deg: np.ndarray, ls: np.ndarray, ms: np.ndarray,
             return tup[(lsum % 2 == 0) & (msum == 0)]
         return tup
 
+    # invariant functions of order >= 2 end with an index whose m and l
+    # parity are fixed by the prefix (sum m = 0, sum l even): the A indices of
+    # each (m, l parity), ascending, enumerate just those
+    invariant = not vec and sphL is None
+    by_mp = {}
+    if invariant:
+        for mv in np.unique(ms):
+            for par in (0, 1):
+                by_mp[(int(mv), par)] = np.nonzero((ms == mv) & (ls % 2 == par))[0]
+
+    def last_invariant(tup, dsum, msum, lsum, parts):
+        """The last index of invariant tuples: per prefix row, the A indices
+        v in [lo, hi) with m_v = -msum and l_v = lsum (mod 2), ascending, so
+        rows and their completions come out in lexicographic order."""
+        lo = tup[:, -1]
+        hi = np.searchsorted(deg, maxdeg - dsum, side="right")
+        tm = -msum
+        tp = lsum % 2
+        cnt = np.zeros(len(tup), dtype=np.int64)
+        first = np.zeros(len(tup), dtype=np.int64)
+        keys = tm * 2 + tp
+        for key in np.unique(keys):
+            sel = np.nonzero(keys == key)[0]
+            P = by_mp.get((int(key // 2), int(key % 2)))
+            if P is None or not len(P):
+                continue
+            a = np.searchsorted(P, lo[sel], side="left")
+            b = np.searchsorted(P, hi[sel], side="left")
+            cnt[sel] = np.maximum(b - a, 0)
+            first[sel] = a
+        total = int(cnt.sum())
+        if total == 0:
+            return
+        off = np.concatenate([[0], np.cumsum(cnt)])
+        rows = np.repeat(np.arange(len(tup)), cnt)
+        j = np.arange(total) - off[rows]
+        v = np.empty(total, dtype=np.int64)
+        for key in np.unique(keys[cnt > 0]):
+            P = by_mp[(int(key // 2), int(key % 2))]
+            m_ = keys[rows] == key
+            v[m_] = P[first[rows[m_]] + j[m_]]
+        parts.append(np.concatenate([tup[rows], v[:, None]], axis=1))
+
     def extend(tup, dsum, msum, lsum, t, k, parts):
         """Enumerate the completions of the prefixes `tup` (t indices each)
         to order k; append the filtered tuples to `parts` in order."""
@@ -131,6 +174,14 @@ def gensparse_ordered(deg: np.ndarray, ls: np.ndarray, ms: np.ndarray,
         hi = np.searchsorted(deg, (maxdeg - dsum) / rem, side="right")
         cnt = np.maximum(hi - lo, 0)
         total = int(cnt.sum())
+        if invariant and k >= 2 and t == k - 1 and total > 0:
+            if total > chunk_rows and len(tup) > 1:
+                h = len(tup) // 2
+                extend(tup[:h], dsum[:h], msum[:h], lsum[:h], t, k, parts)
+                extend(tup[h:], dsum[h:], msum[h:], lsum[h:], t, k, parts)
+            else:
+                last_invariant(tup, dsum, msum, lsum, parts)
+            return
         if total == 0:
             return
         if total > chunk_rows and len(tup) > 1:
