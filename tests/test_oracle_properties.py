@@ -2,8 +2,9 @@
 A = sum_j phi(X_j) (test/test_1pbasis.jl:45-53), O(3) + permutation
 invariance of B (test/test_symmbasis.jl:63-68), linear independence
 (test/test_symmbasis.jl:102-110), :standard == :naive == sum(B .* c)
-(test/test_linearmodel.jl:50-79) and finite-difference gradients
-(test/test_pibasis.jl:78-96)."""
+(test/test_linearmodel.jl:50-79), finite-difference gradients
+(test/test_pibasis.jl:78-96) and categorical-species invariance
+(test/test_discrete.jl:80-88)."""
 import numpy as np
 import pytest
 
@@ -77,3 +78,20 @@ def test_gradient_fd(model):
     for h in (1e-2, 1e-3, 1e-4, 1e-5):
         errs.append(abs((F(h) - F(-h)) / (2 * h) - np.sum(G * U)))
     assert min(errs) < 1e-7 * max(1.0, abs(np.sum(G * U)))
+
+
+def test_categorical_species_invariance(oracle_mod):
+    # two species (test/test_discrete.jl:80-88): B is invariant under O(3)
+    # and under permutations that move each neighbour's species with it, and
+    # depends on which neighbour carries which species
+    spec = symmetric_basis(3, 6, maxL=6, rcut=2.5, nspecies=2)
+    orc = oracle_mod.Oracle(spec, random_coefficients(spec, 2))
+    b = random_batch(1, 10, 10, rlo=0.5, rhi=2.5, nspecies=2, seed=5)
+    B1 = orc.basis(b.offsets, b.rr, b.species)
+    for k in range(10):
+        Q = _rot(20 + k) * (-1) ** k
+        perm = np.random.default_rng(k).permutation(10)
+        B2 = orc.basis(b.offsets, b.rr[perm] @ Q.T, b.species[perm])
+        assert np.allclose(B1, B2, rtol=1e-10, atol=1e-12)
+    flipped = (1 - b.species).astype(b.species.dtype)
+    assert not np.allclose(B1, orc.basis(b.offsets, b.rr, flipped), rtol=1e-6)
