@@ -5,7 +5,6 @@ import os
 import socket
 
 import numpy as np
-import pytest
 
 from ace_gb300.configs import random_batch
 from ace_gb300.replicas import local_batch, partition, spec_costs
