@@ -267,7 +267,8 @@ extern "C" int ace_ctx_create(const ace_spec_bundle *s, int32_t prec, int32_t de
         return fail(ACE_ERR_ALLOC);
       }
       ctx->allocs.push_back(ctx->d_uval);
-      if ((rc = pack_coefs(ctx, ctx->d_uval, (int64_t)ur.val.size(), [&](int64_t j) { return ur.val[j]; }))) {
+      rc = pack_coefs(ctx, ctx->d_uval, (int64_t)ur.val.size(), [&](int64_t j) { return ur.val[j]; });
+      if (rc != ACE_OK) {
         g_create_error = ctx->err;
         return fail(rc);
       }

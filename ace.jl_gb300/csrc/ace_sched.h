@@ -98,7 +98,12 @@ inline Schedule build_schedule(int nA, const int32_t *a_n, const int32_t *a_l, c
     for (int64_t k = 0; k < nAA; ++k) {
       const int o = orders[k];
       for (int j = 0; j < o; ++j) t[j] = partner[iAA2iA[k * K + j]];
-      std::sort(t, t + o, std::greater<int32_t>());
+      for (int a = 1; a < o; ++a) {  // descending insertion sort (o <= 6)
+        const int32_t x = t[a];
+        int b = a - 1;
+        while (b >= 0 && t[b] < x) { t[b + 1] = t[b]; --b; }
+        t[b + 1] = x;
+      }
       pkeyed[k] = {tuple_key(t, o), k};
     }
     std::sort(pkeyed.begin(), pkeyed.end(), by_key);
