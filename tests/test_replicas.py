@@ -1,10 +1,11 @@
-"""Replicas on several ranks (CPU, gloo, world size 2): cost-balanced
+"""Replicas on several ranks (CPU, gloo, world sizes 2 and 4): cost-balanced
 contiguous partitions of a batch, the FP64 energy sum over ranks and the
 max-over-ranks timing, with the oracle evaluating each rank's share."""
 import os
 import socket
 
 import numpy as np
+import pytest
 
 from ace_gb300.configs import random_batch
 from ace_gb300.replicas import local_batch, partition, spec_costs
@@ -51,15 +52,16 @@ def _worker(rank, world, port, out):
     dist.destroy_process_group()
 
 
-def test_two_rank_replicas(oracle_mod):
+@pytest.mark.parametrize("world", [2, 4])
+def test_replicas_over_ranks(oracle_mod, world):
     import multiprocessing as mp
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
     port = _free_port()
-    procs = [ctx.Process(target=_worker, args=(r, 2, port, q)) for r in range(2)]
+    procs = [ctx.Process(target=_worker, args=(r, world, port, q)) for r in range(world)]
     for p in procs:
         p.start()
-    res = [q.get(timeout=240) for _ in range(2)]
+    res = [q.get(timeout=240) for _ in range(world)]
     for p in procs:
         p.join(timeout=60)
         assert p.exitcode == 0
@@ -69,5 +71,5 @@ def test_two_rank_replicas(oracle_mod):
     Eall = oracle_mod.Oracle(spec, random_coefficients(spec, seed=1)).evaluate(b.offsets, b.rr)
     for rank, tot, tmax, n in res:
         assert abs(tot - Eall.sum()) <= 1e-10 * max(1.0, abs(Eall.sum()))
-        assert tmax == 2.0
+        assert tmax == float(world)
     assert sum(r[3] for r in res) == b.nenv
