@@ -57,8 +57,9 @@ enum {
 enum {
   ACE_PREC_FP64 = 0,        /* all arithmetic in FP64 */
   ACE_PREC_FP32 = 1,        /* everything in FP32 (per-environment sums in FP64) */
-  ACE_PREC_FP32_BF16X3 = 2, /* FP32, plus split-BF16 (3-pass) tensor-core U*AA for ace_basis */
-  ACE_PREC_LEARNED = 3,     /* reserved: learned radial compression */
+  ACE_PREC_FP32_BF16X3 = 2, /* accepted, evaluates exactly as ACE_PREC_FP32: a split-BF16
+                               tensor-core U*AA would be HBM-bound (U blocks of ~2 rows) */
+  ACE_PREC_LEARNED = 3,     /* reserved; the learned radial form is ace_set_radial_mlp */
   ACE_PREC_FP32X2 = 4       /* energy path (Rn, Ylm, A, AA) in double-float (pairs of FP32
                                with error-free transformations), adjoint and forces in FP32 */
 };
