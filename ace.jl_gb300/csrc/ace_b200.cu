@@ -138,7 +138,10 @@ extern "C" int ace_ctx_create(const ace_spec_bundle *s, int32_t prec, int32_t de
   auto fail = [&](int code) { ace_ctx_destroy(ctx); return code; };
   if (cudaSetDevice(device) != cudaSuccess) { g_create_error = "cudaSetDevice failed"; return fail(ACE_ERR_CUDA); }
   cudaDeviceProp prop;
-  cudaGetDeviceProperties(&prop, device);
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) {
+    g_create_error = "cudaGetDeviceProperties failed";
+    return fail(ACE_ERR_CUDA);
+  }
   ctx->nsm = prop.multiProcessorCount;
   ctx->smem_optin = (int)prop.sharedMemPerBlockOptin;
 
@@ -224,13 +227,19 @@ extern "C" int ace_ctx_create(const ace_spec_bundle *s, int32_t prec, int32_t de
       return fail(ACE_ERR_ALLOC);
     }
     ctx->allocs.push_back(ctx->d_ic);
-    cudaMemset(ctx->d_ic, 0, ctx->ik.size() * csz);
+    if (cudaMemset(ctx->d_ic, 0, ctx->ik.size() * csz) != cudaSuccess) {
+      g_create_error = "cudaMemset failed";
+      return fail(ACE_ERR_CUDA);
+    }
     if (cudaMalloc(&ctx->d_sc, nslot * csz) != cudaSuccess) {
       g_create_error = "cudaMalloc failed";
       return fail(ACE_ERR_ALLOC);
     }
     ctx->allocs.push_back(ctx->d_sc);
-    cudaMemset(ctx->d_sc, 0, nslot * csz);
+    if (cudaMemset(ctx->d_sc, 0, nslot * csz) != cudaSuccess) {
+      g_create_error = "cudaMemset failed";
+      return fail(ACE_ERR_CUDA);
+    }
   }
   // U (host copy for c~ = U^T c; device copy for the basis path)
   if (s->nB > 0) {
@@ -280,7 +289,10 @@ extern "C" int ace_ctx_create(const ace_spec_bundle *s, int32_t prec, int32_t de
     return fail(ACE_ERR_ALLOC);
   }
   ctx->allocs.push_back(ctx->d_status);
-  cudaMemset(ctx->d_status, 0, sizeof(int));
+  if (cudaMemset(ctx->d_status, 0, sizeof(int)) != cudaSuccess) {
+    g_create_error = "cudaMemset failed";
+    return fail(ACE_ERR_CUDA);
+  }
   ctx->ctilde.assign(s->nAA, 0.0);
   if (cudaMallocHost((void **)&ctx->h_status, sizeof(int)) != cudaSuccess) {
     g_create_error = "cudaMallocHost failed";
@@ -806,13 +818,14 @@ extern "C" int ace_autotune(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, 
       const int32_t *sp = input_species(ctx) > 1 ? species : nullptr;
       int rc = launch_energy_forces(ctx, nEnv, offsets, rr, sp, E, dEdrr, st);  // warm-up
       if (rc) continue;
-      cudaEventRecord(e0, st);
-      for (int r = 0; r < reps; ++r) launch_energy_forces(ctx, nEnv, offsets, rr, sp, E, dEdrr, st);
-      cudaEventRecord(e1, st);
-      cudaEventSynchronize(e1);
+      // a candidate counts only when its launches and the timing succeeded
+      bool timed = cudaEventRecord(e0, st) == cudaSuccess;
+      for (int r = 0; r < reps && timed; ++r)
+        timed = launch_energy_forces(ctx, nEnv, offsets, rr, sp, E, dEdrr, st) == ACE_OK;
+      timed = timed && cudaEventRecord(e1, st) == cudaSuccess && cudaEventSynchronize(e1) == cudaSuccess;
       float ms = 0.f;
-      cudaEventElapsedTime(&ms, e0, e1);
-      if (cudaGetLastError() == cudaSuccess && ms < best) { best = ms; best_region = reg; best_items = items; }
+      timed = timed && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess;
+      if (timed && cudaGetLastError() == cudaSuccess && ms < best) { best = ms; best_region = reg; best_items = items; }
     }
   }
   cudaEventDestroy(e0);
