@@ -649,33 +649,48 @@ static int energy_forces_pipelined(ace_ctx *ctx, int64_t nEnv, const int64_t *of
   int32_t *d_sp = wsp ? (int32_t *)(base + o_sp) : nullptr;
   double *d_E = (double *)(base + o_E);
   double *d_G = G ? (double *)(base + o_G) : nullptr;
-  ACE_CUDA(cudaMemcpyAsync(d_off, off, (nEnv + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->s_in));
+  // a failure inside the loop stops issuing work; every stream is drained
+  // before returning, so no copy into the caller's buffers outlives the call
   int err = ACE_OK;
-  int k = 0;
-  for (; k < nchunk; ++k) {
+  auto ck = [&](cudaError_t e, const char *what) {
+    if (e != cudaSuccess && err == ACE_OK) err = ctx_fail(ctx, ACE_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    return err == ACE_OK;
+  };
+  ck(cudaMemcpyAsync(d_off, off, (nEnv + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->s_in), "offsets copy");
+  for (int k = 0; k < nchunk && err == ACE_OK; ++k) {
     const int64_t e0 = nEnv * k / nchunk, e1 = nEnv * (k + 1) / nchunk;
     const int64_t j0 = off[e0], j1 = off[e1];
     if ((err = validate_range(ctx, j0, j1, rr, sp))) break;
     cudaEvent_t ev_in = ctx->pipe_ev[2 * k], ev_comp = ctx->pipe_ev[2 * k + 1];
     if (j1 > j0) {
-      ACE_CUDA(cudaMemcpyAsync(d_rr + 3 * j0, rr + 3 * j0, (j1 - j0) * 3 * sizeof(double), cudaMemcpyHostToDevice,
-                               ctx->s_in));
-      if (wsp)
-        ACE_CUDA(cudaMemcpyAsync(d_sp + j0, sp + j0, (j1 - j0) * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->s_in));
+      if (!ck(cudaMemcpyAsync(d_rr + 3 * j0, rr + 3 * j0, (j1 - j0) * 3 * sizeof(double), cudaMemcpyHostToDevice,
+                              ctx->s_in), "positions copy"))
+        break;
+      if (wsp && !ck(cudaMemcpyAsync(d_sp + j0, sp + j0, (j1 - j0) * sizeof(int32_t), cudaMemcpyHostToDevice,
+                                     ctx->s_in), "species copy"))
+        break;
     }
-    ACE_CUDA(cudaEventRecord(ev_in, ctx->s_in));
-    ACE_CUDA(cudaStreamWaitEvent(ctx->s_comp, ev_in, 0));
+    if (!ck(cudaEventRecord(ev_in, ctx->s_in), "event record") ||
+        !ck(cudaStreamWaitEvent(ctx->s_comp, ev_in, 0), "stream wait"))
+      break;
     if ((err = launch_energy_forces(ctx, e1 - e0, d_off + e0, d_rr, d_sp, d_E + e0, d_G, ctx->s_comp))) break;
-    ACE_CUDA(cudaEventRecord(ev_comp, ctx->s_comp));
-    ACE_CUDA(cudaStreamWaitEvent(ctx->s_out, ev_comp, 0));
-    ACE_CUDA(cudaMemcpyAsync(E + e0, d_E + e0, (e1 - e0) * sizeof(double), cudaMemcpyDeviceToHost, ctx->s_out));
-    if (G && j1 > j0)
-      ACE_CUDA(cudaMemcpyAsync(G + 3 * j0, d_G + 3 * j0, (j1 - j0) * 3 * sizeof(double), cudaMemcpyDeviceToHost,
-                               ctx->s_out));
+    if (!ck(cudaEventRecord(ev_comp, ctx->s_comp), "event record") ||
+        !ck(cudaStreamWaitEvent(ctx->s_out, ev_comp, 0), "stream wait"))
+      break;
+    if (!ck(cudaMemcpyAsync(E + e0, d_E + e0, (e1 - e0) * sizeof(double), cudaMemcpyDeviceToHost, ctx->s_out),
+            "energies copy"))
+      break;
+    if (G && j1 > j0 &&
+        !ck(cudaMemcpyAsync(G + 3 * j0, d_G + 3 * j0, (j1 - j0) * 3 * sizeof(double), cudaMemcpyDeviceToHost,
+                            ctx->s_out), "gradients copy"))
+      break;
   }
-  ACE_CUDA(cudaStreamSynchronize(ctx->s_out));
-  ACE_CUDA(cudaStreamSynchronize(ctx->s_comp));
-  ACE_CUDA(cudaStreamSynchronize(ctx->s_in));
+  const cudaError_t q_out = cudaStreamSynchronize(ctx->s_out);
+  const cudaError_t q_comp = cudaStreamSynchronize(ctx->s_comp);
+  const cudaError_t q_in = cudaStreamSynchronize(ctx->s_in);
+  ck(q_out, "stream synchronize");
+  ck(q_comp, "stream synchronize");
+  ck(q_in, "stream synchronize");
   if (err) return err;
   return read_status(ctx, ctx->s_comp);
 }
