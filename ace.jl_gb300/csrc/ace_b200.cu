@@ -574,17 +574,24 @@ static int drive(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, const doubl
   int rc = ensure_stage(ctx, need);
   if (rc) return rc;
   char *base = (char *)ctx->d_stage;
+  // on a failure after work was issued the stream is drained before
+  // returning, so no copy touches the caller's buffers after the call
+  auto fail_drained = [&](int code, const std::string &msg) {
+    cudaStreamSynchronize(st);
+    return ctx_fail(ctx, code, msg);
+  };
   if (!din) {
-    ACE_CUDA(cudaMemcpyAsync(base + o_off, offsets, (nEnv + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, st));
-    ACE_CUDA(cudaMemcpyAsync(base + o_rr, rr, nNbr * 3 * sizeof(double), cudaMemcpyHostToDevice, st));
+    cudaError_t ce = cudaMemcpyAsync(base + o_off, offsets, (nEnv + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, st);
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(base + o_rr, rr, nNbr * 3 * sizeof(double), cudaMemcpyHostToDevice, st);
     d_off = (const int64_t *)(base + o_off);
     d_rr = (const double *)(base + o_rr);
     if (species && nsp > 1) {
-      ACE_CUDA(cudaMemcpyAsync(base + o_sp, species, nNbr * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+      if (ce == cudaSuccess) ce = cudaMemcpyAsync(base + o_sp, species, nNbr * sizeof(int32_t), cudaMemcpyHostToDevice, st);
       d_sp = (const int32_t *)(base + o_sp);
     } else {
       d_sp = nullptr;
     }
+    if (ce != cudaSuccess) return fail_drained(ACE_ERR_CUDA, std::string("input copy: ") + cudaGetErrorString(ce));
   } else if (nsp == 1) {
     d_sp = nullptr;
   }
@@ -592,12 +599,16 @@ static int drive(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, const doubl
   for (size_t i = 0; i < outs_host_bytes.size(); ++i)
     d_outs[i] = (dout || !outs_host_bytes[i].first) ? outs_host_bytes[i].first : (void *)(base + o_out[i]);
   rc = run(d_off, d_rr, d_sp, d_outs, st);
-  if (rc) return rc;
+  if (rc) {
+    if (!din) cudaStreamSynchronize(st);
+    return rc;
+  }
   if (!dout) {
-    for (size_t i = 0; i < outs_host_bytes.size(); ++i)
+    cudaError_t ce = cudaSuccess;
+    for (size_t i = 0; i < outs_host_bytes.size() && ce == cudaSuccess; ++i)
       if (outs_host_bytes[i].first)
-        ACE_CUDA(cudaMemcpyAsync(outs_host_bytes[i].first, d_outs[i], outs_host_bytes[i].second,
-                                 cudaMemcpyDeviceToHost, st));
+        ce = cudaMemcpyAsync(outs_host_bytes[i].first, d_outs[i], outs_host_bytes[i].second, cudaMemcpyDeviceToHost, st);
+    if (ce != cudaSuccess) return fail_drained(ACE_ERR_CUDA, std::string("output copy: ") + cudaGetErrorString(ce));
   }
   if (!(flags & ACE_ASYNC) || !din || !dout) return read_status(ctx, st);
   return ACE_OK;
