@@ -265,7 +265,7 @@ def mlp_flops_per_neighbour(mlp):
 def run_learned(args, torch, dist, rank, world, local):
     """The learned radial form on the 4-species workload: distil a K = 8
     student from the plain model (FP64 labels), then time the student's
-    energies + forces on held-out environments and judge its error against
+    energies + forces on held-out environments and measure its error against
     the plain FP64 evaluation."""
     from ace_gb300 import learned as LR
     from ace_gb300.configs import random_batch
@@ -303,7 +303,7 @@ def run_learned(args, torch, dist, rank, world, local):
     plain_student = Context(spec, "fp32", device=local)
     cp = LR.fit_coefficients(plain_student, spec, LR.sub_batch(train, 0, 20000), Etr[:20000], forces=forces)
     plain_student.set_params(cp)
-    # judge on the held-out set: FP64 plain evaluation (device path, chunked)
+    # reference on the held-out set: FP64 plain evaluation (device path, chunked)
     off_d = torch.from_numpy(ev.offsets).to(dev)
     rr_d = torch.from_numpy(ev.rr).to(dev)
     sp_d = torch.from_numpy(ev.species).to(dev)
@@ -312,13 +312,13 @@ def run_learned(args, torch, dist, rank, world, local):
     teacher.energy_forces_device(off_d, rr_d, sp_d, E_d, G_d)
     Eref, Gref = E_d.cpu().numpy().copy(), G_d.cpu().numpy().copy()
 
-    def judged():
+    def student_error():
         ctx.energy_forces_device(off_d, rr_d, sp_d, E_d, G_d)
         E, G = E_d.cpu().numpy(), G_d.cpu().numpy()
         e = LR.energy_error(E, Eref)
         e["F_rel_rmse"] = float(np.sqrt(np.mean((G - Gref) ** 2)) / np.sqrt(np.mean(Gref ** 2)))
         return e
-    err_untrained = judged()
+    err_untrained = student_error()
     plain_student.energy_forces_device(off_d, rr_d, sp_d, E_d, G_d)
     Ep, Gp = E_d.cpu().numpy(), G_d.cpu().numpy()
     err_no_network = LR.energy_error(Ep, Eref)
@@ -327,7 +327,7 @@ def run_learned(args, torch, dist, rank, world, local):
     c1, hist = LR.distill(ctx, mlp, spec, train, Etr, c0, steps=dsteps, batch_envs=512, lr=1e-3,
                           refit_every=500, refit_envs=20000, forces=forces)
     t2 = time.perf_counter()
-    err = judged()
+    err = student_error()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream(dev)
     for _ in range(args.warmup):
