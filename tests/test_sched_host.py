@@ -28,7 +28,7 @@ def checker(tmp_path_factory):
 
 
 @pytest.mark.parametrize("args", [(2, 6, 6, 1), (3, 6, 6, 1), (3, 8, 6, 1), (4, 10, 10, 1), (5, 8, 8, 1),
-                                  (3, 6, 6, 3)])
+                                  (3, 6, 6, 3), (4, 8, 8, 2), (6, 7, 7, 1)])
 def test_schedules_match_flat_products(checker, oracle_mod, tmp_path, args):
     o, deg, L, ns = args
     spec = symmetric_basis(o, deg, maxL=L, nspecies=ns)
