@@ -92,3 +92,28 @@ def test_valid_bundle_passes_validation(lib, spec):
     rc, msg, out = create(lib, b, device=10 ** 6)
     assert rc == CUDA and "device" in msg
     assert np.all(keep["orders"] >= 0)
+
+
+def test_every_entry_point_rejects_a_null_context(lib):
+    L = lib.load()
+    n = None
+    calls = {
+        "ace_set_params": (n, n, 0), "ace_set_ctilde": (n, n, 0), "ace_set_params_multi": (n, n, 0, 1),
+        "ace_set_ctilde_complex": (n, n, 0, 1),
+        "ace_energy_forces": (n, 1, n, n, n, n, n, 0, n), "ace_energy": (n, 1, n, n, n, n, 0, n),
+        "ace_energy_forces_multi": (n, 1, n, n, n, n, n, 0, n), "ace_basis": (n, 1, n, n, n, n, n, 0, n),
+        "ace_basis_noalloc": (n, 1, n, n, n, n, n), "ace_adjoint_eval_d": (n, 1, n, n, n, n, n, 0, n),
+        "ace_autotune": (n, 1, n, n, n, n, n, 1, n, n), "ace_sync": (n,), "ace_get_spec_sizes": (n, n),
+        "ace_set_radial_mlp": (n, n), "ace_radial_mlp_params": (n, n, n), "ace_radial_mlp_get_params": (n, n, 0),
+        "ace_radial_mlp_forward": (n, 1, n, n, n, n), "ace_radial_mlp_infer": (n, 1, n, n, n, n),
+        "ace_radial_mlp_backward": (n, 1, n, n, n, n, n, n),
+        "ace_energy_radial_adjoint": (n, 1, n, n, n, n, n, n, n),
+    }
+    for name, args in calls.items():
+        assert getattr(L, name)(*args) == INVALID, name
+    assert L.ace_ctx_destroy(None) == OK
+    assert L.ace_launch_count(None) == 0
+    assert L.ace_last_error_string(None) is not None
+    # the context-free Adam step: argument checks before any launch
+    assert L.ace_adam_step(10, n, n, n, n, 1e-3, 0.9, 0.999, 1e-8, 1, n) == INVALID
+    assert L.ace_adam_step(0, n, n, n, n, 1e-3, 0.9, 0.999, 1e-8, 1, n) == OK
