@@ -256,7 +256,8 @@ int ace_sync(ace_ctx *ctx);
 /* sizes[0..3] = nA, nAA, nB, maxord */
 int ace_get_spec_sizes(const ace_ctx *ctx, int64_t *sizes);
 
-/* Last error message of this context (or of the last failed create when ctx is NULL). */
+/* Last error message of this context (or of the calling thread's last failed create when ctx
+   is NULL). */
 const char *ace_last_error_string(const ace_ctx *ctx);
 
 /* Number of kernel launches this context has issued (for accounting). */
