@@ -50,3 +50,36 @@ def test_header_compiles_as_c99(tmp_path):
                         "-I", os.path.join(root, "include"), os.path.join(root, "tests", "host", "c_consumer.c"),
                         "-o", obj], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_energy_force_kernels_do_not_spill(tmp_path):
+    """The per-type register bounds of the energy/force kernel (ef_min_blocks)
+    leave the item-schedule instantiations of orders 2-5 without local-memory
+    spills (ptxas resource report; the code itself is not read)."""
+    import re
+    import shutil
+    import subprocess
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc not available")
+    src = os.path.join(ROOT, "ace.jl_gb300", "csrc", "ace_launch.cu")
+    r = subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "-Xptxas", "-v",
+                        "-I", os.path.join(ROOT, "include"), "-c", src, "-o", str(tmp_path / "l.o")],
+                       capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stderr[-2000:]
+    cur, report = None, {}
+    for line in r.stderr.splitlines():
+        m = re.search(r"Compiling entry function '(\S+)'", line) or re.search(r"Function properties for (\S+)", line)
+        if m:
+            cur = m.group(1)
+        elif cur and "spill stores" in line:
+            report[cur] = int(re.search(r"(\d+) bytes spill stores", line).group(1))
+    names = list(report)
+    dem = subprocess.run(["c++filt"], input="\n".join(names), capture_output=True, text=True).stdout.splitlines()
+    checked = 0
+    for mangled, d in zip(names, dem):
+        m = re.search(r"ef_kernel<(.+), (\d), 128, true, true, false>", d)
+        if m and 2 <= int(m.group(2)) <= 5:
+            assert report[mangled] == 0, d
+            checked += 1
+    assert checked == 12  # {float, double-float, double} x orders 2..5
