@@ -31,9 +31,31 @@ def deps():
         glob.glob(os.path.join(INCLUDE, "*.h"))
 
 
+_ELF_MACHINE = {"x86_64": 62, "aarch64": 183, "arm64": 183}
+
+
+def built_for_this_host(path: str) -> bool:
+    """True when the shared object at `path` is an ELF file for this host's
+    CPU architecture (a library compiled on another machine is rebuilt)."""
+    import platform
+    import struct
+    want = _ELF_MACHINE.get(platform.machine())
+    try:
+        with open(path, "rb") as f:
+            head = f.read(20)
+    except OSError:
+        return False
+    if len(head) < 20 or head[:4] != b"\x7fELF":
+        return False
+    endian = "<" if head[5] == 1 else ">"
+    machine = struct.unpack(endian + "H", head[18:20])[0]
+    return want is None or machine == want
+
+
 def build(force: bool = False, verbose: bool = False, extra=()) -> str:
-    """Compile every .cu under csrc/ into libace_b200.so (skipped when up to date)."""
-    if not force and os.path.exists(LIB):
+    """Compile every .cu under csrc/ into libace_b200.so (skipped when up to
+    date and built for this host's architecture)."""
+    if not force and os.path.exists(LIB) and built_for_this_host(LIB):
         t = os.path.getmtime(LIB)
         if all(os.path.getmtime(d) <= t for d in deps()):
             return LIB

@@ -120,7 +120,10 @@ extern "C" int ace_ctx_create(const ace_spec_bundle *s, int32_t prec, int32_t de
   std::string why;
   int rc = validate_spec(s, why);
   if (rc != ACE_OK) return ctx_fail(nullptr, rc, why);
-  if (prec != ACE_PREC_FP64 && prec != ACE_PREC_FP32 && prec != ACE_PREC_FP32_BF16X3 && prec != ACE_PREC_FP32X2)
+  if (prec == ACE_PREC_FP32_BF16X3)
+    return ctx_fail(nullptr, ACE_ERR_UNSUPPORTED,
+                    "precision mode ACE_PREC_FP32_BF16X3 (split-BF16 tensor-core U*AA) is not built");
+  if (prec != ACE_PREC_FP64 && prec != ACE_PREC_FP32 && prec != ACE_PREC_FP32X2)
     return ctx_fail(nullptr, ACE_ERR_UNSUPPORTED, "precision mode not supported");
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev)
@@ -301,6 +304,9 @@ extern "C" int ace_ctx_create(const ace_spec_bundle *s, int32_t prec, int32_t de
   if (cudaDeviceSynchronize() != cudaSuccess) { g_create_error = "device sync failed"; return fail(ACE_ERR_CUDA); }
   rc = kernels_prepare(ctx);
   if (rc != ACE_OK) { g_create_error = ctx->err; return fail(rc); }
+  // the allocation-free basis entry point's scratch address (its outcome is
+  // reported by ace_basis_noalloc, not here)
+  noalloc_prepare(ctx);
   *out = ctx;
   return ACE_OK;
 }

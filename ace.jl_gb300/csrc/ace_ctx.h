@@ -105,10 +105,17 @@ struct ace_ctx {
   int mlp_grid_f = 0, mlp_grid_b = 0, mlp_grid_tc = 0;
   bool mlp_tc = false;          // tensor-core (BF16) inference of the radial MLP
   size_t mlp_smem_f = 0, mlp_smem_b = 0;
+  int64_t tc_wait_limit = int64_t(1) << 26;  // polls of an MMA completion before giving up
 
   // host-buffer pipeline (copy in, compute, copy out)
   cudaStream_t s_in = nullptr, s_comp = nullptr, s_out = nullptr;
   std::vector<cudaEvent_t> pipe_ev;
+
+  // ace_basis_noalloc: device address of the static scratch array, looked up
+  // at context creation (noalloc_rc != 0: the look-up failed, noalloc_err why)
+  void *noalloc_scratch = nullptr;
+  int noalloc_rc = 0;
+  std::string noalloc_err;
 
   std::vector<void *> allocs;
   int64_t launches = 0;
@@ -138,6 +145,9 @@ int learned_radials(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const double
                     cudaStream_t st, bool infer = true);
 int launch_radial_adjoint(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const double *rr, const int32_t *sp,
                           double *E, double *G, float *GR, cudaStream_t st);
+// ace_noalloc.cu: the static scratch's device address for this context's
+// device (called by ace_ctx_create; the outcome is kept in the context)
+int noalloc_prepare(ace_ctx *ctx);
 int launch_adjoint_eval_d(ace_ctx *ctx, int64_t nEnv, const int64_t *off_d, const int64_t *off_h,
                           const double *rr, const int32_t *sp, const double *w, double *out, cudaStream_t st);
 }  // namespace ace

@@ -20,6 +20,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <string>
 #include <vector>
 
@@ -71,6 +72,7 @@ struct MLPArgs {
   const float *wj;        // backward: per-neighbour weight (NULL = 1)
   float *gW;              // backward: accumulated parameter gradient
   int *status;
+  int64_t wait_limit;     // tensor-core kernel: polls of an MMA completion before giving up
 };
 
 struct Feat {
@@ -541,7 +543,7 @@ __global__ void __launch_bounds__(128) mlp_fwd_tc_kernel(MLPArgs a) {
     }
     // a wait that gives up leaves the phase pending (waited on again before
     // the TMEM is freed); the block agrees on the outcome
-    const bool done = __syncthreads_and(mbar_wait(mbar, phase, limit) ? 1 : 0) != 0;
+    const bool done = __syncthreads_and(mbar_wait(mbar, phase, a.wait_limit) ? 1 : 0) != 0;
     if (done) phase ^= 1u;
     tc_fence_after();
     return done;
@@ -642,8 +644,10 @@ __global__ void __launch_bounds__(128) mlp_fwd_tc_kernel(MLPArgs a) {
     }
   }
   if (!ok) {
+    // the MMAs still in flight complete before their TMEM is freed (bounded
+    // by the full limit even when a shorter one was given for the waits above)
     if (tid == 0) atomicOr(a.status, ACE_STATUS_TIMEOUT);
-    mbar_wait(mbar, phase, limit);  // the MMAs still in flight, bounded
+    mbar_wait(mbar, phase, limit);
   }
   tc_fence_before();
   __syncthreads();
@@ -660,6 +664,7 @@ static MLPArgs mlp_args(const ace_ctx *ctx) {
   a.xs = (float)(2.0 / (ctx->mlp_tmax - ctx->tl));
   a.tp = ctx->tp; a.pl = ctx->pl; a.pr = ctx->pr;
   a.status = ctx->d_status;
+  a.wait_limit = ctx->tc_wait_limit;
   return a;
 }
 
@@ -675,6 +680,14 @@ static size_t bwd_smem(const ace_ctx *ctx) {
 }
 
 int mlp_prepare(ace_ctx *ctx) {
+  // polls of a tensor-core completion before the kernel gives up and sets
+  // ACE_STATUS_TIMEOUT; ACE_B200_TC_WAIT_LIMIT lowers it (0 makes every wait
+  // give up at once: the failure path is then exercised without a fault)
+  ctx->tc_wait_limit = int64_t(1) << 26;
+  if (const char *wl = getenv("ACE_B200_TC_WAIT_LIMIT")) {
+    const long long v = atoll(wl);
+    if (v >= 0 && v < ctx->tc_wait_limit) ctx->tc_wait_limit = v;
+  }
   // tensor-core inference when the inputs fit one MMA K step (ACE_B200_MLP=fp32: CUDA cores)
   const char *menv = getenv("ACE_B200_MLP");
   ctx->mlp_tc = ctx->mlpD <= TC_K1 && ctx->mlpC <= TC_N3 && ctx->mlpC % 4 == 0 &&

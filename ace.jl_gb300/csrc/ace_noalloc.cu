@@ -16,7 +16,11 @@
 // memory that every GPU which loads this library holds until the process
 // exits.  Its name is only a host-side handle: the device address is obtained
 // once per device with cudaGetSymbolAddress (with that device current) and
-// passed to the kernels.  The first call on a device performs this set-up.
+// passed to the kernels.  ace_ctx_create performs this set-up (it allocates
+// anyway), so that loading the module onto the device -- which takes device
+// memory for the array and the code -- happens there and never inside
+// ace_basis_noalloc.  A device reset (cudaDeviceReset) invalidates the saved
+// address: the library must not be used across one.
 //
 // All calls share the array.  Each call overwrites every scratch element it
 // reads before reading it, so nothing has to start at zero; calls that overlap
@@ -45,35 +49,56 @@ int fail(ace_ctx *ctx, int code, const char *msg) {
   return code;
 }
 
-// Once per device, with that device current: the scratch array's device
-// address and the shared-memory opt-in of this file's kernel instances.
-int setup(ace_ctx *ctx, void **out) {
+}  // namespace
+
+namespace ace {
+// Called by ace_ctx_create with the context's device current: once per
+// device, the scratch array's device address and the shared-memory opt-in of
+// this file's kernel instances.  The result is kept in the context
+// (noalloc_scratch, or noalloc_rc / noalloc_err when the set-up failed), so
+// that ace_basis_noalloc itself makes no CUDA call that could load code.
+int noalloc_prepare(ace_ctx *ctx) {
   std::lock_guard<std::mutex> lk(g_mu);
   const int dev = ctx->device;
-  if (dev < 0 || dev >= ACE_NOALLOC_MAX_DEVICES) return fail(ctx, ACE_ERR_UNSUPPORTED, "device index too large");
+  ctx->noalloc_scratch = nullptr;
+  if (dev < 0 || dev >= ACE_NOALLOC_MAX_DEVICES) {
+    ctx->noalloc_err = "device index too large for the static scratch table";
+    return ctx->noalloc_rc = ACE_ERR_UNSUPPORTED;
+  }
   if (!g_ready[dev]) {
     void *p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_aa_scratch);
     if (e != cudaSuccess) {
-      ctx->err = std::string("cudaGetSymbolAddress failed: ") + cudaGetErrorString(e);
-      return ACE_ERR_CUDA;
+      ctx->noalloc_err = std::string("cudaGetSymbolAddress failed: ") + cudaGetErrorString(e);
+      return ctx->noalloc_rc = ACE_ERR_CUDA;
     }
     const void *fns[] = {(const void *)ace::aa_kernel<double, double>, (const void *)ace::aa_kernel<ace::df, double>,
                          (const void *)ace::aa_kernel<float, float>};
     for (const void *f : fns) {
       e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, ctx->smem_optin);
       if (e != cudaSuccess) {
-        ctx->err = std::string("cudaFuncSetAttribute failed: ") + cudaGetErrorString(e);
-        return ACE_ERR_CUDA;
+        ctx->noalloc_err = std::string("cudaFuncSetAttribute failed: ") + cudaGetErrorString(e);
+        return ctx->noalloc_rc = ACE_ERR_CUDA;
+      }
+    }
+    // load the code of the B = U AA kernels now (lazy module loading would
+    // otherwise load it, taking device memory, at their first launch)
+    const void *ub[] = {(const void *)ace::ub_kernel<double>, (const void *)ace::ub_kernel<float>};
+    for (const void *f : ub) {
+      cudaFuncAttributes fa;
+      e = cudaFuncGetAttributes(&fa, f);
+      if (e != cudaSuccess) {
+        ctx->noalloc_err = std::string("cudaFuncGetAttributes failed: ") + cudaGetErrorString(e);
+        return ctx->noalloc_rc = ACE_ERR_CUDA;
       }
     }
     g_scratch_ptr[dev] = p;
     g_ready[dev] = true;
   }
-  *out = g_scratch_ptr[dev];
-  return ACE_OK;
+  ctx->noalloc_scratch = g_scratch_ptr[dev];
+  return ctx->noalloc_rc = ACE_OK;
 }
-}  // namespace
+}  // namespace ace
 
 extern "C" int ace_basis_noalloc(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, const double *rr,
                                  const int32_t *species, double *B, void *stream) {
@@ -90,11 +115,13 @@ extern "C" int ace_basis_noalloc(ace_ctx *ctx, int64_t nEnv, const int64_t *offs
     return fail(ctx, ACE_ERR_UNSUPPORTED,
                 "ace_basis_noalloc: one environment's AA vector (nAA x element size) exceeds the 16 MiB "
                 "static scratch; use ace_basis");
+  if (ctx->noalloc_rc != ACE_OK || !ctx->noalloc_scratch) {
+    ctx->err = "ace_basis_noalloc set-up failed at context creation: " + ctx->noalloc_err;
+    return ctx->noalloc_rc != ACE_OK ? ctx->noalloc_rc : ACE_ERR_CUDA;
+  }
   if (nEnv == 0) return ACE_OK;
   if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, ACE_ERR_CUDA, "cudaSetDevice failed");
-  void *scratch = nullptr;
-  int rc = setup(ctx, &scratch);
-  if (rc) return rc;
+  void *scratch = ctx->noalloc_scratch;
   cudaStream_t st = (cudaStream_t)stream;
   const int64_t per = std::min<int64_t>((int64_t)(ACE_NOALLOC_SCRATCH_BYTES / per_env), nEnv);
   void *fa = f32 ? (void *)aa_kernel<float, float>

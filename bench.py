@@ -1,27 +1,27 @@
 """Benchmark: environment evaluations per second (energy + forces) on one GB300.
 
-Workload (the configuration the metric is quoted on): a single-species
-invariant ACE model of correlation order 4, total degree 12 (Ylm L <= 12,
-Rn = orthogonal polynomials in ((1+r0)/(1+r))^2, r0 = 1, cutoff 5.0),
-100,000 environments with U{20..60} neighbours at radii U[0.8, 5.0] and
-isotropic directions, coefficients c_k ~ N(0,1)/(1+deg_k)^2, seeded.
+Workload (the configuration the metric's target is stated on): a
+single-species invariant ACE model of correlation order 5, total degree 16
+(Ylm L <= 16, Rn = orthogonal polynomials in ((1+r0)/(1+r))^2, r0 = 1,
+cutoff 5.0; 488 A, 1,310,316 AA and 55,420 B functions), 500,000
+environments x 30 neighbours at radii U[0.8, 5.0] and isotropic directions,
+coefficients c_k ~ N(0,1)/(1+deg_k)^2, seeded.
 
-A step evaluates E and dE/drr for all environments.  `value` times the kernel
-with inputs resident in HBM (L2 flushed between steps); `e2e` times the
-C-ABI call with pinned host buffers (host->device copy of positions,
-device->host copy of energies and gradients inside the timed region).
+A step evaluates E and dE/drr for all environments.  `value` times the
+chosen form's kernel with inputs resident in HBM (L2 flushed between steps);
+`e2e` times the C-ABI call with pinned host buffers (host->device copy of
+positions, device->host copy of energies and gradients inside the timed
+region).  The plain FP64 form is timed on a prefix of the batch
+(``fp64_envs``) to keep its steps within seconds.
 
-`--workload` selects one of the larger measured configurations instead
+`--workload` selects another measured configuration instead
 (``learned_4sp`` distils and times the learned radial form on the 4-species
-model):
-``ord5_deg16`` (order 5, degree 16, L 16; 500,000 environments x 30
-neighbours), ``ord4_deg10_4sp`` (4 species, order 4, degree 10, L 10;
-250,000 environments whose neighbour counts are 60 % U{40..80} and 40 %
+model): ``ord4_deg12`` (order 4, degree 12, L 12; 100,000 environments with
+U{20..60} neighbours), ``ord4_deg10_4sp`` (4 species, order 4, degree 10,
+L 10; 250,000 environments whose neighbour counts are 60 % U{40..80} and 40 %
 U{8..20}, species uniform) and ``ord4_deg14_4sp`` (the same at degree 14:
 24.8M AA functions; run it with few steps, e.g. ``--steps 2 --warmup 1``).
-On those the FP64 form is timed on a prefix of the batch (``fp64_envs``) to
-keep a step within seconds, and ``autotune_envs`` bounds the autotuner's
-batch.
+``autotune_envs`` bounds the autotuner's batch.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--workload NAME]
 """
@@ -46,18 +46,19 @@ CHOSEN = "fp32x2"
 WORKLOADS = {
     "ord4_deg12": dict(name="ace-invariant ord4 deg12 L12, 100k envs, J~U{20..60}",
                        maxorder=4, maxdeg=12, maxL=12, nspecies=1, nenv=100_000, jlo=20, jhi=60, seed=2024,
-                       fp64_envs=None),
+                       fp64_envs=None, autotune_envs=20_000),
     "ord5_deg16": dict(name="ace-invariant ord5 deg16 L16, 500k envs, J=30",
                        maxorder=5, maxdeg=16, maxL=16, nspecies=1, nenv=500_000, jlo=30, jhi=30, seed=2024,
-                       fp64_envs=20_000),
+                       fp64_envs=20_000, autotune_envs=20_000),
     "ord4_deg10_4sp": dict(name="ace-invariant 4 species ord4 deg10 L10, 250k envs, J 60% U{40..80} / 40% U{8..20}",
                            maxorder=4, maxdeg=10, maxL=10, nspecies=4, nenv=250_000, jlo=8, jhi=80, seed=2024,
-                           bimodal=(0.6, (40, 80), (8, 20)), fp64_envs=20_000),
+                           bimodal=(0.6, (40, 80), (8, 20)), fp64_envs=20_000, autotune_envs=20_000),
     "ord4_deg14_4sp": dict(name="ace-invariant 4 species ord4 deg14 L14, 250k envs, J 60% U{40..80} / 40% U{8..20}",
                            maxorder=4, maxdeg=14, maxL=14, nspecies=4, nenv=250_000, jlo=8, jhi=80, seed=2024,
                            bimodal=(0.6, (40, 80), (8, 20)), fp64_envs=2_000, autotune_envs=5_000),
 }
-WORKLOAD = WORKLOADS["ord4_deg12"]
+DEFAULT_WORKLOAD = "ord5_deg16"
+WORKLOAD = WORKLOADS[DEFAULT_WORKLOAD]
 
 
 def dist_info():
@@ -78,6 +79,24 @@ def build_workload(nenv=None, rank=0):
     b = random_batch(nenv or W["nenv"], W["jlo"], W["jhi"], nspecies=W["nspecies"], seed=W["seed"] + 7919 * rank,
                      bimodal=W.get("bimodal"))
     return spec, c, b
+
+
+def workload_config(b, world):
+    """The `config` object of the JSON line, identical in both arms for the
+    same workload: what is evaluated, not how."""
+    W = WORKLOAD
+    io_mb = (2 * b.rr.nbytes + b.offsets.nbytes + 8 * b.nenv
+             + (0 if b.species is None else b.species.nbytes)) / 1e6
+    return {"workload": W["name"], "nenv_per_gpu": int(b.nenv), "nnbr_per_gpu": int(b.nnbr),
+            "parallelism": f"replicas x{world}",
+            "l2": f"GPU steps flush L2 (256 MB write) between timed steps; inputs + outputs {io_mb:.0f} MB per step"}
+
+
+def algorithmic_bytes(b):
+    """Bytes the evaluation must move per step: positions, offsets and species
+    in, energies and gradients out."""
+    return (2 * b.rr.nbytes + b.offsets.nbytes + 8 * b.nenv
+            + (0 if b.species is None else b.species.nbytes))
 
 
 def _ptr_dev(t):
@@ -221,13 +240,19 @@ def run_reference(args):
     oracle.build()
     orc = oracle.Oracle(spec, c)
     nthreads = os.cpu_count()
-    # each step: a bounded sample of the workload (a contiguous block of environments)
-    n = 256
-    off = b.offsets[:n + 1]
-    sp = None if b.species is None else b.species[:off[-1]]
-    t0 = time.perf_counter(); orc.energy_forces(off, b.rr[:off[-1]], sp, nthreads=nthreads)
-    dt = time.perf_counter() - t0
-    n = int(min(b.nenv, max(256, n * 6.0 / max(dt, 1e-3))))
+    # each step: a bounded sample of the workload (a contiguous block of
+    # environments) of about `step_s` seconds
+    step_s = 4.0
+    n = 2 * nthreads
+    while True:
+        off = b.offsets[:n + 1]
+        sp = None if b.species is None else b.species[:off[-1]]
+        t0 = time.perf_counter(); orc.energy_forces(off, b.rr[:off[-1]], sp, nthreads=nthreads)
+        dt = time.perf_counter() - t0
+        if dt >= 0.5 or n >= b.nenv:
+            break
+        n = min(b.nenv, 4 * n)
+    n = int(min(b.nenv, max(nthreads, n * step_s / max(dt, 1e-3))))
     times = []
     for step in range(args.warmup + args.steps):
         e0 = (step * n) % (b.nenv - n + 1)
@@ -243,7 +268,7 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / len(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded)", "config": {"workload": WORKLOAD["name"], "sample_envs_per_step": n},
+            "data": "synthetic (seeded)", "config": workload_config(b, world), "sample_envs_per_step": n,
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
                              "sample": f"{n} environments per step, E+F, FP64 CPU restatement of the "
                                        f"reference evaluator (Julia is not available), {nthreads} threads"},
@@ -416,10 +441,10 @@ def main():
     ap.add_argument("--distill-steps", type=int, default=None, help="learned form: distillation steps")
     ap.add_argument("--plain-pretrain", action="store_true",
                     help="learned form: pretrain on the species-blind polynomial radials")
-    ap.add_argument("--workload", default="ord4_deg12", choices=sorted(WORKLOADS) + ["learned_4sp"])
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS) + ["learned_4sp"])
     args = ap.parse_args()
     global WORKLOAD
-    WORKLOAD = WORKLOADS.get(args.workload, WORKLOADS["ord4_deg12"])
+    WORKLOAD = WORKLOADS.get(args.workload, WORKLOADS[DEFAULT_WORKLOAD])
     if args.impl == "reference":
         return run_reference(args)
 
@@ -498,11 +523,13 @@ def main():
     # on the first 20,000 environments
     ctx32 = Context(spec, "fp32", device=local)
     ctx32.set_params(c)
-    nt = min(nenv, 20_000, WORKLOAD.get("autotune_envs") or nenv)
+    nt = min(nenv, WORKLOAD.get("autotune_envs") or nenv)
     ctx32.autotune(off_d[:nt + 1], rr_d, sp_d, E_d[:nt], G_d, reps=1, stream=stream.cuda_stream)
     torch.cuda.synchronize()
-    t32p, _ = timed(ctx32, args.steps, args.warmup)
+    k32 = max(1, min(args.steps, 5))
+    t32p, _ = timed(ctx32, k32, min(args.warmup, 2))
     err32 = errors()
+    del ctx32
     # the chosen form: double-float energy path, FP32 adjoint and forces,
     # launch configuration picked by the autotuner on this batch
     ctx = Context(spec, CHOSEN, device=local)
@@ -519,7 +546,7 @@ def main():
 
     # energies only (evaluate without grad_config), chosen form
     E_only = {}
-    for _ in range(max(1, args.warmup)):
+    for _ in range(max(1, min(args.warmup, 2))):
         ctx.lib.ace_energy(ctx.h, nenv, _ptr_dev(off_d), _ptr_dev(rr_d), _ptr_dev(sp_d), _ptr_dev(E_d), 3 | 4,
                            stream.cuda_stream)
     torch.cuda.synchronize()
@@ -544,7 +571,7 @@ def main():
     basis = {}
     Bref = None
     for name, cx in (("basis_fp64", ctx64), ("basis_fp32x2", ctx)):
-        for _ in range(max(1, args.warmup)):
+        for _ in range(max(1, min(args.warmup, 2))):
             cx.basis_device(off_d[:nbe + 1], rr_d, sp_d, B_d, stream=stream.cuda_stream, sync=False)
         torch.cuda.synchronize()
         tb = 0.0
@@ -570,6 +597,7 @@ def main():
 
     # e2e through the C ABI with pinned host buffers
     e2e = None
+    ke2e, we2e = max(1, min(args.steps, 5)), max(1, min(args.warmup, 2))
     if not args.no_e2e:
         off_h = torch.from_numpy(b.offsets).pin_memory().numpy()
         rr_h = torch.from_numpy(b.rr).pin_memory().numpy()
@@ -584,21 +612,22 @@ def main():
             rc = lib.ace_energy_forces(ctx.h, nenv, _ptr(off_h), _ptr(rr_h), _ptr(sp_h), _ptr(E_h), _ptr(G_h), 0,
                                        None)
             assert rc == 0, lib.ace_last_error_string(ctx.h)
-        for _ in range(args.warmup):
+        for _ in range(we2e):
             call()
         if world > 1:
             dist.barrier()
         tt = 0.0
-        for _ in range(args.steps):
+        for _ in range(ke2e):
             flush.zero_(); torch.cuda.synchronize()
             t0 = time.perf_counter(); call(); tt += time.perf_counter() - t0
         if world > 1:
             t = torch.tensor([tt], dtype=torch.float64, device=dev)
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             tt = float(t.item())
-        e2e = {"value": nenv * args.steps * world / tt, "unit": UNIT,
+        e2e = {"value": nenv * ke2e * world / tt, "unit": UNIT,
                "h2d_bytes_per_step": int(off_h.nbytes + rr_h.nbytes + (0 if sp_h is None else sp_h.nbytes)),
-               "d2h_bytes_per_step": int(E_h.nbytes + G_h.nbytes)}
+               "d2h_bytes_per_step": int(E_h.nbytes + G_h.nbytes), "steps": ke2e, "warmup": we2e,
+               "call": "ace_energy_forces with pinned host buffers (flags 0): copies in, kernel, copies out"}
 
     if rank != 0:
         if world > 1:
@@ -608,26 +637,30 @@ def main():
     Jmean = nnbr / nenv
     fl = flops_per_env(spec, Jmean) * nenv
     achieved = fl / (t32 / args.steps) / 1e12
+    # DRAM bytes (read + write) per environment of the chosen kernel, from an
+    # ncu capture of this workload (profiles/), scaled to this launch
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", "ef_kernel_fp32x2_traffic.json")
-    if os.path.exists(tpath) and args.workload == "ord4_deg12":
+    tpath = os.path.join(ROOT, "profiles", f"ef_kernel_fp32x2_traffic_{args.workload}.json")
+    if os.path.exists(tpath):
         tr = json.load(open(tpath))
         traffic = tr["dram_bytes_per_env"] * nenv
     roof = {"bound": "fp32", "achieved": achieved, "peak": peaks["fp32_tflops"], "unit": "TFLOP/s",
             "frac": achieved / peaks["fp32_tflops"], "traffic": traffic,
+            "algorithmic_bytes": algorithmic_bytes(b),
             "kernel": "ef_kernel<df, float> (fused 1p basis, A, item-schedule AA energy + adjoint, forces)",
             "peak_source": "measured in this run: cuBLAS SGEMM 8192^3, TF32 off (CUDA-core FP32)",
             "flops_per_env": fl / nenv}
     cpu = None if args.no_cpu else cpu_baseline(spec, c, b)
+    v64 = n64 * k64 * world / t64
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32x2", "data": "synthetic (seeded)",
-            "config": {"workload": WORKLOAD["name"], "nenv_per_gpu": nenv, "nnbr_per_gpu": nnbr,
-                       "form": "fp32x2: Rn, Ylm, A and the AA energy in double-float (FP32 pairs), adjoint and forces in FP32",
-                       "l2": "flushed (256 MB write) between timed steps", "parallelism": f"replicas x{world}",
-                       "autotuned": {"region_kb": tuned % 1000, "schedule": "items" if tuned >= 1000 else "trie"}},
-            "forms": {"fp64": {"value": n64 * k64 * world / t64, "ms_per_step": 1e3 * t64 / k64, "envs": n64},
-                      "fp32": {"value": nenv * args.steps * world / t32p, "ms_per_step": 1e3 * t32p / args.steps,
+            "config": workload_config(b, world),
+            "form": "fp32x2: Rn, Ylm, A and the AA energy in double-float (FP32 pairs), adjoint and forces in FP32",
+            "autotuned": {"region_kb": tuned % 1000, "schedule": "items" if tuned >= 1000 else "trie"},
+            "chosen_over_fp64": value / v64,
+            "forms": {"fp64": {"value": v64, "ms_per_step": 1e3 * t64 / k64, "envs": n64},
+                      "fp32": {"value": nenv * k32 * world / t32p, "ms_per_step": 1e3 * t32p / k32,
                                "error": err32},
                       "fp32x2": {"value": value, "ms_per_step": ms, "error": err}, **E_only, **basis},
             "error": err, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,

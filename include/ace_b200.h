@@ -57,8 +57,7 @@ enum {
 enum {
   ACE_PREC_FP64 = 0,        /* all arithmetic in FP64 */
   ACE_PREC_FP32 = 1,        /* everything in FP32 (per-environment sums in FP64) */
-  ACE_PREC_FP32_BF16X3 = 2, /* accepted, evaluates exactly as ACE_PREC_FP32: a split-BF16
-                               tensor-core U*AA would be HBM-bound (U blocks of ~2 rows) */
+  ACE_PREC_FP32_BF16X3 = 2, /* reserved: ace_ctx_create rejects it with ACE_ERR_UNSUPPORTED */
   ACE_PREC_LEARNED = 3,     /* reserved; the learned radial form is ace_set_radial_mlp */
   ACE_PREC_FP32X2 = 4       /* energy path (Rn, Ylm, A, AA) in double-float (pairs of FP32
                                with error-free transformations), adjoint and forces in FP32 */
@@ -164,11 +163,14 @@ int ace_adjoint_eval_d(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, const
    nothing: inputs and B must be device pointers; its scratch is a 16 MiB
    static device array held by every GPU that loads the library.  Specs whose
    per-environment AA vector (nAA x 8 bytes, or x 4 in FP32 mode) exceeds
-   16 MiB are rejected with ACE_ERR_UNSUPPORTED.  The first call on a device
-   looks up the array's device address; make that first call before any
-   stream capture.  Runs asynchronously on `stream` (ace_sync reports the
-   kernels' status).  All calls share the scratch: calls that overlap on the
-   GPU race and must be serialised by the caller. */
+   16 MiB are rejected with ACE_ERR_UNSUPPORTED, as is the learned radial
+   form.  ace_ctx_create looks up the array's device address and loads this
+   entry point's device code, so only context creation allocates: every call
+   of ace_basis_noalloc, the first included, allocates nothing.  The saved
+   address does not survive a cudaDeviceReset of the device.  Runs
+   asynchronously on `stream` (ace_sync reports the kernels' status).  All
+   calls share the scratch: calls that overlap on the GPU race and must be
+   serialised by the caller. */
 int ace_basis_noalloc(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, const double *rr,
                       const int32_t *species, double *B, void *stream);
 

@@ -28,10 +28,23 @@ def build(force: bool = False) -> str:
     """Compile liboracle.so in place (gcc, OpenMP, no FMA contraction)."""
     so = os.path.join(_HERE, "liboracle.so")
     src = os.path.join(_HERE, "ace_oracle.c")
-    if force or not os.path.exists(so) or os.path.getmtime(so) < os.path.getmtime(src):
+    if force or not os.path.exists(so) or os.path.getmtime(so) < os.path.getmtime(src) or not _native(so):
         subprocess.run(["make", "-C", _HERE, "-B", "liboracle.so"], check=True,
                        stdout=subprocess.DEVNULL)
     return so
+
+
+def _native(path: str) -> bool:
+    """True when the shared object is an ELF file for this host's CPU (one
+    compiled on another machine is rebuilt)."""
+    import platform
+    import struct
+    want = {"x86_64": 62, "aarch64": 183, "arm64": 183}.get(platform.machine())
+    with open(path, "rb") as f:
+        head = f.read(20)
+    if len(head) < 20 or head[:4] != b"\x7fELF":
+        return False
+    return want is None or struct.unpack("<H" if head[5] == 1 else ">H", head[18:20])[0] == want
 
 
 class _Spec(C.Structure):

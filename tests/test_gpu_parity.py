@@ -4,7 +4,7 @@ Tolerances (relative to the largest magnitude of the compared quantity):
   FP64 mode: energies 1e-12, gradients 1e-10, basis 1e-12
   FP32 mode (plain FP32 products, no compensation): energies 3e-5, gradients 1e-4
   FP32X2 mode (double-float energy path, FP32 adjoint): energies 1e-6 (the bar
-  for the chosen form), gradients 1e-4
+  for the chosen form), gradients 1e-5
 """
 import numpy as np
 import pytest
@@ -15,7 +15,7 @@ from ace_gb300.spec import random_coefficients, symmetric_basis
 pytestmark = pytest.mark.gpu
 
 TOL = {"fp64": dict(E=1e-12, G=1e-10, B=1e-12), "fp32": dict(E=3e-5, G=1e-4, B=1e-5),
-       "fp32x2": dict(E=1e-6, G=1e-4, B=1e-11)}
+       "fp32x2": dict(E=1e-6, G=1e-5, B=1e-11)}
 
 
 def relerr(a, b):
@@ -363,7 +363,7 @@ def test_full_size_order4_degree12(lib, oracle_mod):
     E64, G64 = c64.energy_forces(b.offsets, b.rr)
     E, G = cx2.energy_forces(b.offsets, b.rr)
     assert energy_relerr(E, E64) <= 1e-6
-    assert relerr(G, G64) <= 1e-4
+    assert relerr(G, G64) <= TOL["fp32x2"]["G"]
     # oracle on a sample of 300 environments spread over the batch
     idx = np.random.default_rng(0).choice(b.nenv, 300, replace=False)
     off = np.concatenate([[0], np.cumsum(np.diff(b.offsets)[idx])])
@@ -376,14 +376,14 @@ def test_full_size_order4_degree12(lib, oracle_mod):
     for Q in (_rotation(1), -_rotation(2)):
         Er, Gr = cx2.energy_forces(b.offsets, b.rr @ Q.T)
         assert energy_relerr(Er, E) <= 1e-6
-        assert relerr(Gr, G @ Q.T) <= 1e-4
+        assert relerr(Gr, G @ Q.T) <= 2 * TOL["fp32x2"]["G"]
     # permutation of the neighbours inside every environment
     rng = np.random.default_rng(3)
     perm = np.concatenate([b.offsets[e] + rng.permutation(b.offsets[e + 1] - b.offsets[e])
                            for e in range(b.nenv)])
     Ep, Gp = cx2.energy_forces(b.offsets, b.rr[perm])
     assert energy_relerr(Ep, E) <= 1e-6
-    assert relerr(Gp, G[perm]) <= 1e-4
+    assert relerr(Gp, G[perm]) <= 2 * TOL["fp32x2"]["G"]
 
 
 def test_host_pipeline(lib, oracle_mod):
