@@ -15,7 +15,7 @@ ACE_ERR_ALLOC = 3
 ACE_ERR_KERNEL = 4
 ACE_ERR_UNSUPPORTED = 5
 
-PREC = {"fp64": 0, "fp32": 1, "fp32_bf16x3": 2, "fp32x2": 4}
+PREC = {"fp64": 0, "fp32": 1, "fp32_bf16x3": 2, "fp32x2": 4, "fp32c": 5}
 
 ACE_INPUTS_ON_DEVICE = 1
 ACE_OUTPUTS_ON_DEVICE = 2

@@ -108,6 +108,7 @@ template <> struct Arith<float> {
   __device__ __forceinline__ static float one() { return 1.0f; }
   __device__ __forceinline__ static float sqrt_(float x) { return sqrtf(x); }
   __device__ __forceinline__ static float hi(float x) { return x; }
+  __device__ __forceinline__ static float lo(float) { return 0.0f; }
   __device__ __forceinline__ static double to_double(float x) { return (double)x; }
   __device__ __forceinline__ static bool positive(float x) { return x > 0.0f; }
 };
@@ -118,6 +119,7 @@ template <> struct Arith<double> {
   __device__ __forceinline__ static double one() { return 1.0; }
   __device__ __forceinline__ static double sqrt_(double x) { return sqrt(x); }
   __device__ __forceinline__ static double hi(double x) { return x; }
+  __device__ __forceinline__ static double lo(double) { return 0.0; }
   __device__ __forceinline__ static double to_double(double x) { return x; }
   __device__ __forceinline__ static bool positive(double x) { return x > 0.0; }
 };
@@ -141,6 +143,7 @@ template <> struct Arith<df> {
     return {h, l};
   }
   __device__ __forceinline__ static float hi(df x) { return x.hi; }
+  __device__ __forceinline__ static float lo(df x) { return x.lo; }
   __device__ __forceinline__ static double to_double(df x) { return (double)x.hi + (double)x.lo; }
   __device__ __forceinline__ static bool positive(df x) { return x.hi > 0.0f; }
 };

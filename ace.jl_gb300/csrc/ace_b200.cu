@@ -123,14 +123,19 @@ extern "C" int ace_ctx_create(const ace_spec_bundle *s, int32_t prec, int32_t de
   if (prec == ACE_PREC_FP32_BF16X3)
     return ctx_fail(nullptr, ACE_ERR_UNSUPPORTED,
                     "precision mode ACE_PREC_FP32_BF16X3 (split-BF16 tensor-core U*AA) is not built");
-  if (prec != ACE_PREC_FP64 && prec != ACE_PREC_FP32 && prec != ACE_PREC_FP32X2)
+  if (prec != ACE_PREC_FP64 && prec != ACE_PREC_FP32 && prec != ACE_PREC_FP32X2 && prec != ACE_PREC_FP32_COMP)
     return ctx_fail(nullptr, ACE_ERR_UNSUPPORTED, "precision mode not supported");
+  // the compensated form is the double-float form except for its
+  // single-property energy/force kernel
+  const bool comp = (prec == ACE_PREC_FP32_COMP);
+  if (comp) prec = ACE_PREC_FP32X2;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev)
     return ctx_fail(nullptr, ACE_ERR_CUDA, "no such CUDA device");
   ace_ctx *ctx = new ace_ctx();
   ctx->device = device;
   ctx->prec = prec;
+  ctx->comp = comp;
   ctx->nR = s->nR; ctx->nA = s->nA; ctx->nAA = s->nAA; ctx->nB = s->nB;
   ctx->maxord = s->maxord; ctx->nspecies = s->nspecies;
   ctx->pl = s->pl; ctx->pr = s->pr; ctx->tp = s->tp;
@@ -233,6 +238,17 @@ extern "C" int ace_ctx_create(const ace_spec_bundle *s, int32_t prec, int32_t de
     if (cudaMemset(ctx->d_ic, 0, ctx->ik.size() * csz) != cudaSuccess) {
       g_create_error = "cudaMemset failed";
       return fail(ACE_ERR_CUDA);
+    }
+    if (comp) {
+      if (cudaMalloc((void **)&ctx->d_ic32, ctx->ik.size() * sizeof(float)) != cudaSuccess) {
+        g_create_error = "cudaMalloc failed";
+        return fail(ACE_ERR_ALLOC);
+      }
+      ctx->allocs.push_back(ctx->d_ic32);
+      if (cudaMemset(ctx->d_ic32, 0, ctx->ik.size() * sizeof(float)) != cudaSuccess) {
+        g_create_error = "cudaMemset failed";
+        return fail(ACE_ERR_CUDA);
+      }
     }
     if (cudaMalloc(&ctx->d_sc, nslot * csz) != cudaSuccess) {
       g_create_error = "cudaMalloc failed";
@@ -359,6 +375,11 @@ static int push_ctilde(ace_ctx *ctx) {
     return ctx->ik[j] < 0 ? 0.0 : ctx->iw[j] * ctx->ctilde[ctx->ik[j]];
   });
   if (rc) return rc;
+  if (ctx->comp) {
+    std::vector<float> c(ctx->ik.size());
+    for (size_t j = 0; j < c.size(); ++j) c[j] = ctx->ik[j] < 0 ? 0.f : (float)(ctx->iw[j] * ctx->ctilde[ctx->ik[j]]);
+    ACE_CUDA(cudaMemcpy(ctx->d_ic32, c.data(), c.size() * sizeof(float), cudaMemcpyHostToDevice));
+  }
   const int64_t n = (int64_t)ctx->sslot.size();
   auto val = [&](int64_t j) { return ctx->sslot[j] < 0 ? 0.0 : ctx->sw[j] * ctx->ctilde[ctx->sslot[j]]; };
   if (ctx->prec == ACE_PREC_FP64) {
@@ -834,7 +855,9 @@ extern "C" int ace_autotune(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, 
   ACE_CUDA(cudaSetDevice(ctx->device));
   cudaStream_t st = (cudaStream_t)stream;
   const int regions[] = {16, 24, 32, 40, 48, 64};
+  // the compensated form exists for the item schedule only
   const bool variants[] = {true, false};
+  const int nvariants = ctx->comp ? 1 : 2;
   float best = 1e30f;
   int best_region = ctx->region_kb;
   bool best_items = ctx->use_items;
@@ -842,7 +865,8 @@ extern "C" int ace_autotune(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, 
   ACE_CUDA(cudaEventCreate(&e0));
   ACE_CUDA(cudaEventCreate(&e1));
   reps = std::max(1, std::min(reps, 20));
-  for (bool items : variants) {
+  for (int vi = 0; vi < nvariants; ++vi) {
+    const bool items = variants[vi];
     for (int reg : regions) {
       ctx->use_items = items;
       ctx->region_kb = reg;

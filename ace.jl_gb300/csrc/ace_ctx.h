@@ -50,6 +50,10 @@ struct ace_ctx {
   std::vector<uint8_t> sw;     // slot -> weight
   // item schedule (ace_sched.h build_items)
   bool use_items = true;
+  // compensated form (ACE_PREC_FP32_COMP): prec is ACE_PREC_FP32X2 for every
+  // other path; the single-property item kernel reads FP32 coefficients d_ic32
+  bool comp = false;
+  float *d_ic32 = nullptr;     // [(G+1) * item_n] coefficients in FP32
   int64_t item_n = 0;
   uint4 *d_irec = nullptr;
   void *d_ic = nullptr;        // [(G+1) * item_n] coefficients in the energy type
@@ -129,6 +133,8 @@ int launch_energy_forces(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const d
                          const void *ic = nullptr, double c0 = 0.0, bool cpx = false);
 // complex-coefficient (item schedule) energy/force kernels (ace_launch_cplx.cu)
 void *ef_func_cplx(const ace_ctx *ctx, bool grad);
+// compensated-form energy/force kernels (ace_launch_comp.cu)
+void *ef_func_comp(const ace_ctx *ctx);
 int launch_basis(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const double *rr,
                  const int32_t *sp, double *B, double *dB, cudaStream_t st);
 int launch_dbasis(ace_ctx *ctx, int64_t nEnv, const int64_t *off_d, const int64_t *off_h, const double *rr,

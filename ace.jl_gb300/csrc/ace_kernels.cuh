@@ -232,10 +232,26 @@ template <typename TE, int K> constexpr int ef_min_blocks() {
          : K <= 4 ? (std::is_same<TE, df>::value ? 5 : std::is_same<TE, double>::value ? 4 : 7)
                   : (std::is_same<TE, df>::value ? 4 : std::is_same<TE, double>::value ? 3 : 5);
 }
-template <typename TE, typename TG, int K, int NT, bool GRAD, bool ITEMS, bool CPX = false>
-__global__ void __launch_bounds__(NT, ef_min_blocks<TE, CPX ? K + 1 : K>()) ef_kernel(EFArgs a) {
+// COMP (compensated form; TE = df, TG = float, item schedule): A is built in
+// double-float as in the fp32x2 form, but the correlation products run in
+// FP32 on A_hi = the FP32 rounding of A, with FP32 coefficients, and each
+// item's energy term is added to a double-float accumulator.  The rounding
+// A_lo = A - A_hi is put back to first order after the adjoint pass:
+// E = E(A_hi) + Re sum_i dE/dA_i(A_hi) A_lo_i, the adjoint being the one the
+// forces need anyway.  The remaining error is the FP32 rounding of the
+// products, which does not add coherently over the terms.
+// resident CTAs per SM of the compensated form: FP32 item state plus the
+// double-float A build and energy accumulator (no spills at orders 2-5)
+template <int K> constexpr int comp_min_blocks() { return EF_MIN_BLOCKS > 0 ? EF_MIN_BLOCKS : K <= 4 ? 6 : K == 5 ? 5 : 4; }
+template <typename TE, typename TG, int K, int NT, bool GRAD, bool ITEMS, bool CPX = false, bool COMP = false>
+__global__ void __launch_bounds__(NT, COMP ? comp_min_blocks<K>() : ef_min_blocks<TE, CPX ? K + 1 : K>())
+    ef_kernel(EFArgs a) {
   static_assert(ITEMS || !CPX, "complex coefficients need the item schedule");
+  static_assert(!COMP || (ITEMS && GRAD && !CPX && std::is_same<TE, df>::value && std::is_same<TG, float>::value),
+                "the compensated form is the double-float A with FP32 item products and adjoint");
   constexpr bool SAME = std::is_same<TE, TG>::value;
+  // arithmetic type of the correlation products
+  using TL = std::conditional_t<COMP, float, TE>;
   extern __shared__ __align__(16) unsigned char sm[];
   const EFLayout lay = ef_layout(a.ntab, a.nRs, a.L, a.nA, a.chunkE, a.chunkG, a.npriv, NT, sizeof(TE),
                                  sizeof(TG), SAME, a.Rext != nullptr);
@@ -299,6 +315,9 @@ __global__ void __launch_bounds__(NT, ef_min_blocks<TE, CPX ? K + 1 : K>()) ef_k
       }
     };
     TE eacc = Arith<TE>::zero();
+    // the correlation phase reads A in its own arithmetic type
+    const cpx<TL> *AL;
+    if constexpr (COMP) AL = (const cpx<TL> *)AG; else AL = (const cpx<TL> *)AE;
     if constexpr (!ITEMS) {
     cpx<TE> H[K + 1], Ac[K + 1];
     cpx<TG> bar[K + 1];
@@ -359,7 +378,7 @@ __global__ void __launch_bounds__(NT, ef_min_blocks<TE, CPX ? K + 1 : K>()) ef_k
       const int lane = tid & 31;
 #endif
       const cpx<TG> gone = {TG(1), TG(0)};
-      const TE ze = Arith<TE>::zero();
+      const TL ze = Arith<TL>::zero();
 #if EF_ITEM_RUNS
       // reverse-mode accumulation along this thread's run of items (sorted
       // by prefix): the open path cur[0..cP) of the prefix trie with, per
@@ -392,9 +411,9 @@ __global__ void __launch_bounds__(NT, ef_min_blocks<TE, CPX ? K + 1 : K>()) ef_k
       for (int64_t f0 = tid; f0 < a.in; f0 += (int64_t)IU * NT) {
         int P[IU], nl[IU], vi[IU][KP], ul[IU][ITEM_G];
         unsigned heads[IU];
-        cpx<TE> bar[IU], H[IU];
+        cpx<TL> bar[IU], H[IU];
         cpx<TG> aG[IU][KP];
-        TE cl[IU][ITEM_G], cli[IU][ITEM_G];
+        TL cl[IU][ITEM_G], cli[IU][ITEM_G];
 #pragma unroll
         for (int u = 0; u < IU; ++u) {
           const int64_t f = f0 + (int64_t)u * NT;
@@ -405,33 +424,36 @@ __global__ void __launch_bounds__(NT, ef_min_blocks<TE, CPX ? K + 1 : K>()) ef_k
           nl[u] = (rc.w >> 20) & 0xf;
           heads[u] = (rc.w >> 24) & 0xff;
           const uint32_t vw[4] = {rc.x, rc.y, rc.z, rc.w};
-          bar[u] = {Arith<TE>::one(), ze};
+          bar[u] = {Arith<TL>::one(), ze};
 #pragma unroll
           for (int d = 0; d < KP; ++d) {
             vi[u][d] = (int)((vw[d >> 1] >> (16 * (d & 1))) & 0xffff);
             aG[u][d] = gone;
             if (d < P[u]) {
-              const cpx<TE> ae = AE[vi[u][d]];
+              const cpx<TL> ae = AL[vi[u][d]];
               bar[u] = (d == 0) ? ae : cmul(bar[u], ae);
               // the adjoint's copy of A (AG = lower(AE)) from the value in registers
               if (GRAD) aG[u][d] = {lower<TG>(ae.re), lower<TG>(ae.im)};
             }
           }
-          H[u] = {ok ? load_coef<TE>(a.ic, f) : ze, (CPX && ok) ? load_coef<TE>(a.ic, (int64_t)(ITEM_G + 1) * a.in + f) : ze};
+          H[u] = {ok ? load_coef<TL>(a.ic, f) : ze, (CPX && ok) ? load_coef<TL>(a.ic, (int64_t)(ITEM_G + 1) * a.in + f) : ze};
 #pragma unroll
           for (int g = 0; g < ITEM_G; ++g) {
             ul[u][g] = (int)((vw[(5 + g) >> 1] >> (16 * ((5 + g) & 1))) & 0xffff);
-            cl[u][g] = ok ? load_coef<TE>(a.ic, (int64_t)(g + 1) * a.in + f) : ze;
-            cli[u][g] = (CPX && ok) ? load_coef<TE>(a.ic, (int64_t)(ITEM_G + 2 + g) * a.in + f) : ze;
+            cl[u][g] = ok ? load_coef<TL>(a.ic, (int64_t)(g + 1) * a.in + f) : ze;
+            cli[u][g] = (CPX && ok) ? load_coef<TL>(a.ic, (int64_t)(ITEM_G + 2 + g) * a.in + f) : ze;
             if (g < nl[u]) {
-              if constexpr (CPX) H[u] = cadd(H[u], cmul(AE[ul[u][g]], cpx<TE>{cl[u][g], cli[u][g]}));
-              else H[u] = cfma(H[u], AE[ul[u][g]], cl[u][g]);
+              if constexpr (CPX) H[u] = cadd(H[u], cmul(AL[ul[u][g]], cpx<TL>{cl[u][g], cli[u][g]}));
+              else H[u] = cfma(H[u], AL[ul[u][g]], cl[u][g]);
             }
           }
         }
 #pragma unroll
         for (int u = 0; u < IU; ++u)
-          if (P[u] > 0) eacc = eacc + re_mul<TE>(bar[u], H[u]);
+          if (P[u] > 0) {
+            if constexpr (COMP) eacc = eacc + df{re_mul<TL>(bar[u], H[u]), 0.0f};
+            else eacc = eacc + re_mul<TE>(bar[u], H[u]);
+          }
         if (GRAD) {
 #if EF_ITEM_RUNS
 #pragma unroll
@@ -530,8 +552,11 @@ __global__ void __launch_bounds__(NT, ef_min_blocks<TE, CPX ? K + 1 : K>()) ef_k
       if (GRAD) close_to(0);
 #endif
     }
-    const double esum = block_sum(lower<double>(eacc), red);
-    if (tid == 0) a.E[e] = a.c0 + esum;
+    double eloc = lower<double>(eacc);
+    if constexpr (!COMP) {
+      const double esum = block_sum(eloc, red);
+      if (tid == 0) a.E[e] = a.c0 + esum;
+    }
     if (!GRAD) continue;
     // private bins -> D (one warp per bin, lanes over threads)
     {
@@ -550,6 +575,17 @@ __global__ void __launch_bounds__(NT, ef_min_blocks<TE, CPX ? K + 1 : K>()) ef_k
         if (lane == 0 && u < a.nA) { D[u].re += sr; D[u].im += si; }
       }
       __syncthreads();
+    }
+    if constexpr (COMP) {
+      // first-order correction for the FP32 rounding of A: Re sum_i D_i A_lo_i
+      for (int i = tid; i < a.nA; i += NT) {
+        const cpx<TE> ae = AE[i];
+        const cpx<TG> d = D[i];
+        eloc += (double)d.re * (double)Arith<TE>::lo(ae.re) - (double)d.im * (double)Arith<TE>::lo(ae.im);
+      }
+      const double esum = block_sum(eloc, red);
+      if (tid == 0) a.E[e] = a.c0 + esum;
+      if (!a.G && !a.GR) continue;  // energies only
     }
     // ---------------- phase 3: forces
     const int lane = tid & 31, w = tid >> 5, nw = NT >> 5;

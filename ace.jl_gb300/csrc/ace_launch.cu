@@ -53,6 +53,10 @@ static void *ub_func(const ace_ctx *ctx) {
   }
 }
 
+// the compensated kernels replace the double-float item kernels for the
+// single-property energy/force calls of a compensated context
+static bool uses_comp(const ace_ctx *ctx) { return ctx->comp && ctx->use_items && !ctx->learned; }
+
 static void type_sizes(const ace_ctx *ctx, int &sE, int &sG, bool &same) {
   switch (ctx->prec) {
     case ACE_PREC_FP64: sE = 8; sG = 8; same = true; break;
@@ -96,13 +100,15 @@ int kernels_prepare(ace_ctx *ctx) {
   }
   ctx->smem = lay.total;
   int occ = 1;
-  for (int g = 0; g < 2; ++g) {
-    void *f = ef_func(ctx, g == 1);
+  for (int g = 0; g < 3; ++g) {
+    if (g == 2 && !uses_comp(ctx)) break;
+    void *f = g == 2 ? ef_func_comp(ctx) : ef_func(ctx, g == 1);
     if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, ctx->smem_optin) != cudaSuccess) {
       ctx->err = "cudaFuncSetAttribute failed";
       return ACE_ERR_CUDA;
     }
-    if (g == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, f, NT, lay.total);
+    // the grid follows the occupancy of the kernel the context's E+F calls run
+    if (g == (uses_comp(ctx) ? 2 : 1)) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, f, NT, lay.total);
   }
   ctx->grid = ctx->nsm * std::max(occ, 1);
   // basis path (AA materialisation)
@@ -142,6 +148,11 @@ int launch_energy_forces(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const d
   EFArgs a = make_args(ctx, nEnv, off, rr, sp, E, G);
   if (ic) { a.ic = ic; a.c0 = c0; }
   void *f = ef_func(ctx, G != nullptr);
+  if (!ic && !cpx && uses_comp(ctx)) {
+    // energies with or without gradients: the correction needs the adjoint
+    f = ef_func_comp(ctx);
+    a.ic = ctx->d_ic32;
+  }
   if (cpx) {
     f = ef_func_cplx(ctx, G != nullptr);
     if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, ctx->smem_optin) != cudaSuccess) {

@@ -42,7 +42,16 @@ sys.path.insert(0, os.path.join(ROOT, "ace.jl_gb300"))
 
 METRIC = "env-evals/s (E+F) on 1 GB300: chosen form vs plain FP64 path at <=1e-6 rel err"
 UNIT = "env/s"
-CHOSEN = "fp32x2"
+# candidates for the chosen form: the fastest whose energies are within the
+# metric's 1e-6 of the FP64 form is timed for `value`
+CANDIDATES = ("fp32c", "fp32x2")
+E_BAR = 1e-6
+FORMS = {
+    "fp32c": ("f32/f32x2", "fp32c: Rn, Ylm and A in double-float (FP32 pairs); AA products, adjoint and forces in FP32 "
+                           "on A rounded to FP32; energy summed in double-float and corrected to first order for that "
+                           "rounding"),
+    "fp32x2": ("f32x2", "fp32x2: Rn, Ylm, A and the AA energy in double-float (FP32 pairs), adjoint and forces in FP32"),
+}
 WORKLOADS = {
     "ord4_deg12": dict(name="ace-invariant ord4 deg12 L12, 100k envs, J~U{20..60}",
                        maxorder=4, maxdeg=12, maxL=12, nspecies=1, nenv=100_000, jlo=20, jhi=60, seed=2024,
@@ -530,19 +539,33 @@ def main():
     t32p, _ = timed(ctx32, k32, min(args.warmup, 2))
     err32 = errors()
     del ctx32
-    # the chosen form: double-float energy path, FP32 adjoint and forces,
-    # launch configuration picked by the autotuner on this batch
-    ctx = Context(spec, CHOSEN, device=local)
-    ctx.set_params(c)
+    # the chosen form: each candidate autotuned on this batch and timed on a
+    # short run; the fastest within the energy bar gets the full timed run
     na = min(nenv, WORKLOAD.get("autotune_envs") or nenv)
-    tuned = ctx.autotune(off_d[:na + 1], rr_d, sp_d, E_d[:na], G_d, reps=1, stream=stream.cuda_stream)
-    torch.cuda.synchronize()
+    cand = {}
+    for form in CANDIDATES:
+        cx = Context(spec, form, device=local)
+        cx.set_params(c)
+        tn = cx.autotune(off_d[:na + 1], rr_d, sp_d, E_d[:na], G_d, reps=1, stream=stream.cuda_stream)
+        torch.cuda.synchronize()
+        kq = max(1, min(args.steps, 2))
+        tq, _ = timed(cx, kq, 1)
+        cand[form] = {"ctx": cx, "tuned": tn, "value": nenv * kq * world / tq, "ms_per_step": 1e3 * tq / kq,
+                      "error": errors()}
+    ok = [f for f in CANDIDATES if cand[f]["error"]["E_rel_max_vs_fp64"] <= E_BAR] or [CANDIDATES[-1]]
+    chosen = max(ok, key=lambda f: cand[f]["value"])
+    ctx, tuned = cand[chosen]["ctx"], cand[chosen]["tuned"]
+    for f in CANDIDATES:
+        if f != chosen:
+            cand[f]["ctx"].close()
     with Clocks(local) as clk:
         t32, launches = timed(ctx, args.steps, args.warmup)
     clocks = clk.summary()
     err = errors()
     value = nenv * args.steps * world / t32
     ms = 1e3 * t32 / args.steps
+    cand[chosen].update(value=value, ms_per_step=ms, error=err)
+    cand_forms = {f: {k: v for k, v in cand[f].items() if k not in ("ctx", "tuned")} for f in CANDIDATES}
 
     # energies only (evaluate without grad_config), chosen form
     E_only = {}
@@ -562,7 +585,7 @@ def main():
         e.synchronize()
         te += s.elapsed_time(e) / 1e3
     ctx.sync()
-    E_only["fp32x2_energy_only"] = {"value": nenv * ke / te, "ms_per_step": 1e3 * te / ke}
+    E_only[f"{chosen}_energy_only"] = {"value": nenv * ke / te, "ms_per_step": 1e3 * te / ke}
 
     # the symmetric basis B = U real(AA) (grad_params, the design matrix), FP64
     # and fp32x2, on a prefix of the batch with B within 4 GB
@@ -570,7 +593,7 @@ def main():
     B_d = torch.empty((nbe, spec.nB), dtype=torch.float64, device=dev)
     basis = {}
     Bref = None
-    for name, cx in (("basis_fp64", ctx64), ("basis_fp32x2", ctx)):
+    for name, cx in (("basis_fp64", ctx64), (f"basis_{chosen}", ctx)):
         for _ in range(max(1, min(args.warmup, 2))):
             cx.basis_device(off_d[:nbe + 1], rr_d, sp_d, B_d, stream=stream.cuda_stream, sync=False)
         torch.cuda.synchronize()
@@ -640,29 +663,30 @@ def main():
     # DRAM bytes (read + write) per environment of the chosen kernel, from an
     # ncu capture of this workload (profiles/), scaled to this launch
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", f"ef_kernel_fp32x2_traffic_{args.workload}.json")
+    tpath = os.path.join(ROOT, "profiles", f"ef_kernel_{chosen}_traffic_{args.workload}.json")
     if os.path.exists(tpath):
         tr = json.load(open(tpath))
         traffic = tr["dram_bytes_per_env"] * nenv
     roof = {"bound": "fp32", "achieved": achieved, "peak": peaks["fp32_tflops"], "unit": "TFLOP/s",
             "frac": achieved / peaks["fp32_tflops"], "traffic": traffic,
             "algorithmic_bytes": algorithmic_bytes(b),
-            "kernel": "ef_kernel<df, float> (fused 1p basis, A, item-schedule AA energy + adjoint, forces)",
+            "kernel": f"ef_kernel<df, float{', COMP' if chosen == 'fp32c' else ''}> (fused 1p basis, A, "
+                      "item-schedule AA energy + adjoint, forces)",
             "peak_source": "measured in this run: cuBLAS SGEMM 8192^3, TF32 off (CUDA-core FP32)",
             "flops_per_env": fl / nenv}
     cpu = None if args.no_cpu else cpu_baseline(spec, c, b)
     v64 = n64 * k64 * world / t64
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32x2", "data": "synthetic (seeded)",
+            "vs_baseline": None, "dtype": FORMS[chosen][0], "data": "synthetic (seeded)",
             "config": workload_config(b, world),
-            "form": "fp32x2: Rn, Ylm, A and the AA energy in double-float (FP32 pairs), adjoint and forces in FP32",
+            "form": FORMS[chosen][1],
             "autotuned": {"region_kb": tuned % 1000, "schedule": "items" if tuned >= 1000 else "trie"},
             "chosen_over_fp64": value / v64,
             "forms": {"fp64": {"value": v64, "ms_per_step": 1e3 * t64 / k64, "envs": n64},
                       "fp32": {"value": nenv * k32 * world / t32p, "ms_per_step": 1e3 * t32p / k32,
                                "error": err32},
-                      "fp32x2": {"value": value, "ms_per_step": ms, "error": err}, **E_only, **basis},
+                      **cand_forms, **E_only, **basis},
             "error": err, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
             "gpu_launches": int(launches), "peaks_measured": peaks}
     print(json.dumps(line), flush=True)

@@ -59,8 +59,13 @@ enum {
   ACE_PREC_FP32 = 1,        /* everything in FP32 (per-environment sums in FP64) */
   ACE_PREC_FP32_BF16X3 = 2, /* reserved: ace_ctx_create rejects it with ACE_ERR_UNSUPPORTED */
   ACE_PREC_LEARNED = 3,     /* reserved; the learned radial form is ace_set_radial_mlp */
-  ACE_PREC_FP32X2 = 4       /* energy path (Rn, Ylm, A, AA) in double-float (pairs of FP32
+  ACE_PREC_FP32X2 = 4,      /* energy path (Rn, Ylm, A, AA) in double-float (pairs of FP32
                                with error-free transformations), adjoint and forces in FP32 */
+  ACE_PREC_FP32_COMP = 5    /* compensated: Rn, Ylm and A in double-float; the correlation
+                               products, adjoint and forces in FP32 on A rounded to FP32, the
+                               energy summed in double-float and corrected to first order for
+                               that rounding (E += Re sum_i dE/dA_i A_lo_i); every other path
+                               as ACE_PREC_FP32X2 */
 };
 
 /* flags for the evaluation calls */

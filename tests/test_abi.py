@@ -62,13 +62,16 @@ def test_energy_force_kernels_do_not_spill(tmp_path):
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
     if not os.path.exists(nvcc):
         pytest.skip("nvcc not available")
-    src = os.path.join(ROOT, "ace.jl_gb300", "csrc", "ace_launch.cu")
-    r = subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "-Xptxas", "-v",
-                        "-I", os.path.join(ROOT, "include"), "-c", src, "-o", str(tmp_path / "l.o")],
-                       capture_output=True, text=True, timeout=900)
-    assert r.returncode == 0, r.stderr[-2000:]
+    err = ""
+    for name in ("ace_launch.cu", "ace_launch_comp.cu"):
+        src = os.path.join(ROOT, "ace.jl_gb300", "csrc", name)
+        r = subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "-Xptxas", "-v",
+                            "-I", os.path.join(ROOT, "include"), "-c", src, "-o", str(tmp_path / "l.o")],
+                           capture_output=True, text=True, timeout=900)
+        assert r.returncode == 0, r.stderr[-2000:]
+        err += r.stderr
     cur, report = None, {}
-    for line in r.stderr.splitlines():
+    for line in err.splitlines():
         m = re.search(r"Compiling entry function '(\S+)'", line) or re.search(r"Function properties for (\S+)", line)
         if m:
             cur = m.group(1)
@@ -78,8 +81,8 @@ def test_energy_force_kernels_do_not_spill(tmp_path):
     dem = subprocess.run(["c++filt"], input="\n".join(names), capture_output=True, text=True).stdout.splitlines()
     checked = 0
     for mangled, d in zip(names, dem):
-        m = re.search(r"ef_kernel<(.+), (\d), 128, true, true, false>", d)
+        m = re.search(r"ef_kernel<(.+), (\d), 128, true, true, false, (false|true)>", d)
         if m and 2 <= int(m.group(2)) <= 5:
             assert report[mangled] == 0, d
             checked += 1
-    assert checked == 12  # {float, double-float, double} x orders 2..5
+    assert checked == 16  # {float, double-float, double, compensated} x orders 2..5

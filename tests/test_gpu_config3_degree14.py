@@ -14,7 +14,8 @@ from ace_gb300.spec import random_coefficients, symmetric_basis
 
 pytestmark = pytest.mark.gpu
 
-TOL = {"fp64": dict(E=1e-12, G=1e-10), "fp32": dict(E=3e-5, G=1e-4), "fp32x2": dict(E=1e-6, G=1e-5)}
+TOL = {"fp64": dict(E=1e-12, G=1e-10), "fp32": dict(E=3e-5, G=1e-4), "fp32x2": dict(E=1e-6, G=1e-5),
+       "fp32c": dict(E=1e-6, G=1e-5)}
 
 
 @pytest.fixture(scope="module")
@@ -26,7 +27,7 @@ def case(oracle_mod):
     return spec, c, b, Eref, Gref
 
 
-@pytest.mark.parametrize("prec", ["fp64", "fp32", "fp32x2"])
+@pytest.mark.parametrize("prec", ["fp64", "fp32", "fp32x2", "fp32c"])
 def test_config3_degree14(case, prec):
     from ace_gb300 import lib as L
     from ace_gb300.build import build

@@ -53,7 +53,7 @@ def _message(ctx):
     return ctx.lib.ace_last_error_string(ctx.h).decode()
 
 
-@pytest.mark.parametrize("prec", ["fp64", "fp32x2"])
+@pytest.mark.parametrize("prec", ["fp64", "fp32x2", "fp32c"])
 @pytest.mark.parametrize("defect", ["nan", "centre"])
 def test_bad_position_on_device(L, oracle_mod, prec, defect):
     torch = pytest.importorskip("torch")

@@ -5,6 +5,8 @@ Tolerances (relative to the largest magnitude of the compared quantity):
   FP32 mode (plain FP32 products, no compensation): energies 3e-5, gradients 1e-4
   FP32X2 mode (double-float energy path, FP32 adjoint): energies 1e-6 (the bar
   for the chosen form), gradients 1e-5
+  FP32C mode (double-float A, FP32 products and adjoint, first-order energy
+  correction): energies 1e-6, gradients 1e-5; its basis path is FP32X2's
 """
 import numpy as np
 import pytest
@@ -15,7 +17,7 @@ from ace_gb300.spec import random_coefficients, symmetric_basis
 pytestmark = pytest.mark.gpu
 
 TOL = {"fp64": dict(E=1e-12, G=1e-10, B=1e-12), "fp32": dict(E=3e-5, G=1e-4, B=1e-5),
-       "fp32x2": dict(E=1e-6, G=1e-5, B=1e-11)}
+       "fp32x2": dict(E=1e-6, G=1e-5, B=1e-11), "fp32c": dict(E=1e-6, G=1e-5, B=1e-11)}
 
 
 def relerr(a, b):
@@ -55,7 +57,7 @@ def get_spec(name):
     return _spec_cache[name]
 
 
-@pytest.mark.parametrize("prec", ["fp64", "fp32", "fp32x2"])
+@pytest.mark.parametrize("prec", ["fp64", "fp32", "fp32x2", "fp32c"])
 @pytest.mark.parametrize("name,nenv,jlo,jhi", [("test", 64, 10, 10), ("cfg1", 1000, 12, 24),
                                                ("cfg2", 200, 20, 60), ("ord5", 100, 20, 40)])
 def test_energy_forces(lib, oracle_mod, prec, name, nenv, jlo, jhi):
@@ -75,7 +77,7 @@ def test_energy_forces(lib, oracle_mod, prec, name, nenv, jlo, jhi):
     assert energy_relerr(E2, Eref) <= TOL[prec]["E"]
 
 
-@pytest.mark.parametrize("prec", ["fp64", "fp32", "fp32x2"])
+@pytest.mark.parametrize("prec", ["fp64", "fp32", "fp32x2", "fp32c"])
 def test_multispecies(lib, oracle_mod, prec):
     spec = symmetric_basis(3, 6, maxL=6, nspecies=3)
     c = random_coefficients(spec, seed=2)
@@ -89,7 +91,7 @@ def test_multispecies(lib, oracle_mod, prec):
     assert relerr(G, Gref) <= TOL[prec]["G"]
 
 
-@pytest.mark.parametrize("prec", ["fp64", "fp32", "fp32x2"])
+@pytest.mark.parametrize("prec", ["fp64", "fp32", "fp32x2", "fp32c"])
 @pytest.mark.parametrize("path", ["fused", "materialised"])
 @pytest.mark.parametrize("name,nenv,ns", [("cfg1", 300, 1), ("cfg2", 40, 1), ("species", 30, 3)])
 def test_basis(lib, oracle_mod, prec, path, name, nenv, ns, monkeypatch):
@@ -238,7 +240,7 @@ def test_adjoint_eval_d(lib, oracle_mod, prec):
     assert relerr(out, ref) <= tol, relerr(out, ref)
 
 
-@pytest.mark.parametrize("prec", ["fp64", "fp32x2"])
+@pytest.mark.parametrize("prec", ["fp64", "fp32x2", "fp32c"])
 def test_multi_property(lib, oracle_mod, prec):
     """Multi-property model (c::Vector{SVector{N}}): each property equals the
     single-property evaluation with that column of coefficients."""
@@ -260,21 +262,24 @@ def test_multi_property(lib, oracle_mod, prec):
     assert Em.shape == (3, 3) and np.allclose(Em, E[:3], rtol=1e-12)
 
 
-def test_autotune_keeps_results(lib, oracle_mod):
+@pytest.mark.parametrize("prec", ["fp32x2", "fp32c"])
+def test_autotune_keeps_results(lib, oracle_mod, prec):
     torch = pytest.importorskip("torch")
     spec = get_spec("cfg1")
     c = random_coefficients(spec, seed=3)
     b = random_batch(2000, 12, 24, seed=8)
     Eref, Gref = oracle_mod.Oracle(spec, c).energy_forces(b.offsets, b.rr)
-    ctx = lib.Context(spec, "fp32x2")
+    ctx = lib.Context(spec, prec)
     ctx.set_params(c)
     off = torch.from_numpy(b.offsets).cuda(); rr = torch.from_numpy(b.rr).cuda()
     E = torch.empty(b.nenv, dtype=torch.float64, device="cuda"); G = torch.empty_like(rr)
     choice = ctx.autotune(off, rr, None, E, G, reps=1)
     assert choice % 1000 in (16, 24, 32, 40, 48, 64)
+    if prec == "fp32c":
+        assert choice >= 1000  # the compensated form runs on the item schedule only
     E2, G2 = ctx.energy_forces(b.offsets, b.rr)
-    assert energy_relerr(E2, Eref) <= TOL["fp32x2"]["E"]
-    assert relerr(G2, Gref) <= TOL["fp32x2"]["G"]
+    assert energy_relerr(E2, Eref) <= TOL[prec]["E"]
+    assert relerr(G2, Gref) <= TOL[prec]["G"]
 
 
 def test_cuda_graph_capture(lib, oracle_mod):
@@ -307,7 +312,7 @@ def test_cuda_graph_capture(lib, oracle_mod):
     assert relerr(G.cpu().numpy(), Gref) <= 1e-10
 
 
-@pytest.mark.parametrize("prec", ["fp64", "fp32", "fp32x2"])
+@pytest.mark.parametrize("prec", ["fp64", "fp32", "fp32x2", "fp32c"])
 def test_order5_degree16(lib, oracle_mod, prec):
     """The order-5 / degree-16 basis (J = 30) against the oracle."""
     spec = get_spec("ord5_deg16")
@@ -323,7 +328,7 @@ def test_order5_degree16(lib, oracle_mod, prec):
     assert relerr(G, Gref) <= TOL[prec]["G"]
 
 
-@pytest.mark.parametrize("prec", ["fp64", "fp32", "fp32x2"])
+@pytest.mark.parametrize("prec", ["fp64", "fp32", "fp32x2", "fp32c"])
 def test_four_species_bimodal(lib, oracle_mod, prec):
     """4 species, order 4 / degree 10, neighbour counts 60 % U{40..80} and
     40 % U{8..20}, against the oracle."""
