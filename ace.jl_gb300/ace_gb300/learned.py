@@ -17,12 +17,16 @@ the teacher by distillation:
    squares on teacher energies of seeded environments and, optionally, on
    the teacher's per-neighbour gradients (c enters both linearly; the
    student basis B and its derivative dB are evaluated on the GPU).
-3. ``distill``: Adam on the MLP parameters against the teacher energies, with
-   c re-fitted every few hundred steps.  The gradient is exact for the
-   energy loss: dL/dR_c(r_j) comes from the energy kernel's adjoint
-   (``ace_energy_radial_adjoint``) and is pushed through the MLP by
-   ``ace_radial_mlp_backward``; the force term is not in the MLP's loss (it
-   would need the adjoint of the adjoint through the correlation products).
+3. ``distill``: Adam on the MLP parameters against the teacher energies and,
+   optionally, the teacher's per-neighbour gradients, with c re-fitted every
+   few hundred steps.  The energy loss gradient is exact: dL/dR_c(r_j) comes
+   from the energy kernel's adjoint (``ace_energy_radial_adjoint``) and is
+   pushed through the MLP by ``ace_radial_mlp_backward``.  The force loss
+   L_F = sum_j |G_j - G*_j|^2 (G_j = dE/drr_j) has the gradient
+   d/dtheta sum_j W_j . G_j with W_j = dL_F/dG_j held fixed, and
+   sum_j W_j . G_j is the derivative of sum_e E_e(rr + eps W) at eps = 0: a
+   Hessian-vector product, formed as the central difference in eps of two
+   exact energy gradients (``force_loss_gradient``, truncation O(eps^2)).
 
 ``LearnedRadialModel`` evaluates the student and sends every environment
 with a neighbour outside the training radii (or a species the MLP was not
@@ -259,6 +263,36 @@ def fit_coefficients(ctx: Context, spec: ACESpec, b: Batch, E_target: np.ndarray
     return np.linalg.solve(Gh, rh)
 
 
+def force_loss_gradient(ctx: Context, g, off, rr, sp, G, Gt, weight, E_buf, GR_buf, disp: float = 1e-2):
+    """Adds to the parameter gradient g the gradient of the force loss
+    weight * mean_j |G_j - Gt_j|^2 / mean |Gt|^2 over one batch (device
+    tensors; G = dE/drr of the learned form at the current parameters).
+
+    With W_j = dL_F/dG_j held fixed, dL_F/dtheta = d/dtheta sum_j W_j . G_j,
+    and sum_j W_j . G_j = d/deps sum_e E_e(rr + eps W) at eps = 0, so the
+    gradient is d/deps of the parameter gradient of the energies summed over
+    the batch: the central difference of the exact energy gradients at
+    rr +- h W, with h chosen so that the largest displacement is `disp`
+    (Angstrom).  Returns the loss value."""
+    torch = _torch()
+    res = G - Gt
+    n3 = res.numel()
+    sf = float((Gt * Gt).mean()) or 1.0
+    W = (2.0 * weight / (n3 * sf)) * res
+    wmax = float(W.abs().max())
+    loss = weight * float((res * res).mean()) / sf
+    if wmax == 0.0:
+        return loss
+    h = disp / wmax
+    n = rr.shape[0]
+    for sgn in (1.0, -1.0):
+        rs = (rr + (sgn * h) * W).contiguous()
+        ctx.energy_radial_adjoint(off, rs, sp, E_buf, None, GR_buf[:n])
+        wj = torch.full((n,), sgn / (2.0 * h), dtype=torch.float32, device=rr.device)
+        ctx.radial_mlp_backward(rs, sp, GR_buf[:n], wj, g)
+    return loss
+
+
 def sub_batch(b: Batch, e0: int, e1: int) -> Batch:
     o0, o1 = int(b.offsets[e0]), int(b.offsets[e1])
     return Batch(b.offsets[e0:e1 + 1] - o0, b.rr[o0:o1], None if b.species is None else b.species[o0:o1])
@@ -266,10 +300,14 @@ def sub_batch(b: Batch, e0: int, e1: int) -> Batch:
 
 def distill(ctx: Context, mlp: RadialMLP, spec: ACESpec, train: Batch, E_train: np.ndarray, c: np.ndarray,
             steps: int = 2000, batch_envs: int = 512, lr: float = 1e-3, refit_every: int = 500,
-            refit_envs: int = 20000, forces=None, log=None):
+            refit_envs: int = 20000, forces=None, force_loss=None, log=None):
     """Adam on the MLP parameters against teacher energies (c fixed between
     ridge re-fits, which also use the teacher gradients `forces` when
-    given, see fit_coefficients); returns (c, history)."""
+    given, see fit_coefficients); returns (c, history).
+
+    force_loss = (bf, Gt, weight, batch_envs): each step also adds the
+    gradient of weight * the relative mean-square force error on a batch of
+    the environments of bf (teacher gradients Gt), see force_loss_gradient."""
     torch = _torch()
     dev = torch.device("cuda", ctx.device)
     off_d = torch.from_numpy(train.offsets).to(dev)
@@ -288,6 +326,18 @@ def distill(ctx: Context, mlp: RadialMLP, spec: ACESpec, train: Batch, E_train: 
     hist = []
     rng = np.random.default_rng(11)
     refit = sub_batch(train, 0, min(refit_envs, nEnv))
+    if force_loss is not None:
+        fb, fG, fw, fbe = force_loss
+        f_off = torch.from_numpy(fb.offsets).to(dev)
+        f_rr = torch.from_numpy(fb.rr).to(dev)
+        f_sp = None if fb.species is None else torch.from_numpy(fb.species).to(dev)
+        f_Gt = torch.from_numpy(np.ascontiguousarray(fG, dtype=np.float64).reshape(-1, 3)).to(dev)
+        fbe = min(fbe, fb.nenv)
+        fmax = int(np.max(fb.offsets[fbe:] - fb.offsets[:-fbe])) if fb.nenv > fbe else int(fb.offsets[-1])
+        f_E = torch.empty(fbe, dtype=torch.float64, device=dev)
+        f_G = torch.empty((fmax, 3), dtype=torch.float64, device=dev)
+        if fmax > GR.shape[0]:
+            GR = torch.empty((fmax, mlp.C), dtype=torch.float32, device=dev)
     for it in range(steps):
         e0 = int(rng.integers(0, max(1, nEnv - batch_envs)))
         e1 = min(nEnv, e0 + batch_envs)
@@ -303,13 +353,23 @@ def distill(ctx: Context, mlp: RadialMLP, spec: ACESpec, train: Batch, E_train: 
         wj = torch.repeat_interleave(w, J[e0:e1]).to(torch.float32)
         tr.g.zero_()
         ctx.radial_mlp_backward(rr_b, sp_b, GR[:o1 - o0], wj, tr.g)
+        floss = 0.0
+        if force_loss is not None:
+            q0 = int(rng.integers(0, max(1, fb.nenv - fbe)))
+            q1 = min(fb.nenv, q0 + fbe)
+            p0, p1 = int(fb.offsets[q0]), int(fb.offsets[q1])
+            fo = (f_off[q0:q1 + 1] - p0).contiguous()
+            fr = f_rr[p0:p1]
+            fs = None if f_sp is None else f_sp[p0:p1]
+            ctx.energy_radial_adjoint(fo, fr, fs, f_E[:q1 - q0], f_G[:p1 - p0], GR[:p1 - p0])
+            floss = force_loss_gradient(ctx, tr.g, fo, fr, fs, f_G[:p1 - p0], f_Gt[p0:p1], fw, f_E[:q1 - q0], GR)
         step_lr = lr * (0.1 if it >= 0.8 * steps else 1.0)
         tr.adam(step_lr)
         if it % 100 == 0 or it == steps - 1:
             loss = float((res * res).mean()) / var
-            hist.append((it, loss))
+            hist.append((it, loss, floss) if force_loss is not None else (it, loss))
             if log:
-                log(f"distill {it}: rel mse {loss:.3e}")
+                log(f"distill {it}: rel mse {loss:.3e} force {floss:.3e}")
         if refit_every and (it + 1) % refit_every == 0 and it + 1 < steps:
             torch.cuda.synchronize()
             c = fit_coefficients(ctx, spec, refit, E_train[:refit.nenv], forces=forces)

@@ -85,7 +85,7 @@ struct ace_ctx {
   // launch configuration chosen at create time (and by ace_autotune)
   int region_kb = 40;          // shared region for neighbour slabs / private adjoint bins
   int nt = 128, chunkE = 32, chunkG = 16, npriv = 32, grid = 0;
-  size_t smem = 0;
+  size_t smem = 0, smem_comp = 0;
   int aa_chunk = 32, aa_grid = 0;
   size_t aa_smem = 0;
   // fused symmetric basis (ace_sched.h build_urows); false: AA materialised

@@ -93,8 +93,11 @@ struct EFLayout {
   int slabE, slabG;
 };
 
+// comp: the compensated form keeps A as two FP32 arrays, A_hi (the adjoint's
+// and the products' copy, AG) and A_lo, in the AE region (no separate AG)
 inline __host__ __device__ EFLayout ef_layout(int ntab, int nR, int L, int nA, int chunkE, int chunkG,
-                                              int npriv, int nt, int sE, int sG, bool same, bool radj = false) {
+                                              int npriv, int nt, int sE, int sG, bool same, bool radj = false,
+                                              bool comp = false) {
   EFLayout l;
   size_t o = 0;
   const int szP = size_p(L), nY = size_y(L);
@@ -104,7 +107,7 @@ inline __host__ __device__ EFLayout ef_layout(int ntab, int nR, int L, int nA, i
   l.aiy = o; o = al16(o + (size_t)nA * 2);
   l.amu = o; o = al16(o + (size_t)nA * 2);
   l.AE = o; o = al16(o + (size_t)nA * 2 * sE);
-  l.AG = same ? l.AE : o; if (!same) o = al16(o + (size_t)nA * 2 * sG);
+  l.AG = (same || comp) ? l.AE : o; if (!same && !comp) o = al16(o + (size_t)nA * 2 * sG);
   l.D = o; o = al16(o + (size_t)nA * 2 * sG);
   const int ch = chunkE > chunkG ? chunkE : chunkG;
   l.pos = o; o = al16(o + (size_t)ch * 4 * sG);
@@ -163,14 +166,36 @@ __device__ __forceinline__ double block_sum(double v, double *red) {
 // Neighbours are staged `chunk` at a time; thread (jj, m) = (t / (L+1),
 // t % (L+1)) evaluates column m of Y for neighbour jj (and R_n when m == 0),
 // then one thread per A entry accumulates.  Requires chunk * (L+1) <= blockDim.
-template <typename T>
+// SPLIT (T = df): A is stored as two FP32 arrays, A_hi = ((cpx<float> *)A)[i]
+// and A_lo = ((cpx<float> *)A)[nA + i], instead of nA double-float pairs.
+template <typename T, bool SPLIT>
+__device__ __forceinline__ cpx<T> a_load(const cpx<T> *A, int nA, int i) {
+  if constexpr (SPLIT) {
+    const cpx<float> h = ((const cpx<float> *)A)[i], l = ((const cpx<float> *)A)[nA + i];
+    return {Arith<T>::from_pair(h.re, l.re), Arith<T>::from_pair(h.im, l.im)};
+  } else {
+    return A[i];
+  }
+}
+template <typename T, bool SPLIT>
+__device__ __forceinline__ void a_store(cpx<T> *A, int nA, int i, cpx<T> v) {
+  if constexpr (SPLIT) {
+    ((cpx<float> *)A)[i] = {Arith<T>::hi(v.re), Arith<T>::hi(v.im)};
+    ((cpx<float> *)A)[nA + i] = {Arith<T>::lo(v.re), Arith<T>::lo(v.im)};
+  } else {
+    A[i] = v;
+  }
+}
+
+template <typename T, bool SPLIT = false>
 __device__ __forceinline__ void build_A(const EFArgs &a, const Tables<T> &tb, int64_t o0, int J, int chunk,
                                         int SE, const int16_t *s_an, const int16_t *s_aiy, const int16_t *s_amu,
                                         int *ssp, T *slab, cpx<T> *A) {
+  static_assert(!SPLIT || std::is_same<T, df>::value, "split storage holds double-float values");
   const int tid = threadIdx.x, nt = blockDim.x;
   const int LP1 = a.L + 1;
   const int jj = tid / LP1, m = tid - jj * LP1;
-  for (int i = tid; i < a.nA; i += nt) A[i] = {Arith<T>::zero(), Arith<T>::zero()};
+  for (int i = tid; i < a.nA; i += nt) a_store<T, SPLIT>(A, a.nA, i, {Arith<T>::zero(), Arith<T>::zero()});
   for (int c0 = 0; c0 < J; c0 += chunk) {
     const int nc = min(chunk, J - c0);
     __syncthreads();
@@ -198,14 +223,14 @@ __device__ __forceinline__ void build_A(const EFArgs &a, const Tables<T> &tb, in
     __syncthreads();
     for (int i = tid; i < a.nA; i += nt) {
       const int n = s_an[i], iy = s_aiy[i], mu = s_amu[i];
-      cpx<T> acc = A[i];
+      cpx<T> acc = a_load<T, SPLIT>(A, a.nA, i);
       for (int q = 0; q < nc; ++q) {
         if (a.nspecies > 1 && ssp[q] != mu) continue;
         const T *sl = slab + (size_t)q * SE;
         const cpx<T> Y = ((const cpx<T> *)(sl + a.nRs))[iy];
         acc = cfma(acc, Y, sl[n]);
       }
-      A[i] = acc;
+      a_store<T, SPLIT>(A, a.nA, i, acc);
     }
   }
   __syncthreads();
@@ -247,14 +272,15 @@ template <typename TE, typename TG, int K, int NT, bool GRAD, bool ITEMS, bool C
 __global__ void __launch_bounds__(NT, COMP ? comp_min_blocks<K>() : ef_min_blocks<TE, CPX ? K + 1 : K>())
     ef_kernel(EFArgs a) {
   static_assert(ITEMS || !CPX, "complex coefficients need the item schedule");
-  static_assert(!COMP || (ITEMS && GRAD && !CPX && std::is_same<TE, df>::value && std::is_same<TG, float>::value),
-                "the compensated form is the double-float A with FP32 item products and adjoint");
+  static_assert(!COMP || (ITEMS && GRAD && !CPX && EF_ITEM_RUNS && std::is_same<TE, df>::value &&
+                          std::is_same<TG, float>::value),
+                "the compensated form is the double-float A with FP32 item products and the run adjoint");
   constexpr bool SAME = std::is_same<TE, TG>::value;
   // arithmetic type of the correlation products
   using TL = std::conditional_t<COMP, float, TE>;
   extern __shared__ __align__(16) unsigned char sm[];
   const EFLayout lay = ef_layout(a.ntab, a.nRs, a.L, a.nA, a.chunkE, a.chunkG, a.npriv, NT, sizeof(TE),
-                                 sizeof(TG), SAME, a.Rext != nullptr);
+                                 sizeof(TG), SAME, a.Rext != nullptr, COMP);
   TE *tabE = (TE *)(sm + lay.tabE);
   TG *tabG = (TG *)(sm + lay.tabG);
   int16_t *s_an = (int16_t *)(sm + lay.an);
@@ -294,10 +320,11 @@ __global__ void __launch_bounds__(NT, COMP ? comp_min_blocks<K>() : ef_min_block
     }
     const int J = (int)(o1 - o0);
     // ---------------- phase 1
-    build_A<TE>(a, tbE, o0, J, a.chunkE, lay.slabE, s_an, s_aiy, s_amu, ssp, (TE *)(sm + lay.slab), AE);
+    build_A<TE, COMP>(a, tbE, o0, J, a.chunkE, lay.slabE, s_an, s_aiy, s_amu, ssp, (TE *)(sm + lay.slab), AE);
     if (GRAD) {
       for (int i = tid; i < a.nA; i += NT) {
-        if (!SAME) AG[i] = {lower<TG>(AE[i].re), lower<TG>(AE[i].im)};
+        // (the compensated form's A_hi already is the adjoint's copy)
+        if (!SAME && !COMP) AG[i] = {lower<TG>(AE[i].re), lower<TG>(AE[i].im)};
         D[i] = {TG(0), TG(0)};
       }
       for (int i = tid; i < npriv * NT; i += NT) priv[i] = {TG(0), TG(0)};
@@ -431,7 +458,9 @@ __global__ void __launch_bounds__(NT, COMP ? comp_min_blocks<K>() : ef_min_block
             aG[u][d] = gone;
             if (d < P[u]) {
               const cpx<TL> ae = AL[vi[u][d]];
-              bar[u] = (d == 0) ? ae : cmul(bar[u], ae);
+              // (the compensated form takes the prefix product from the
+              // adjoint's path products Q below instead)
+              if constexpr (!COMP) bar[u] = (d == 0) ? ae : cmul(bar[u], ae);
               // the adjoint's copy of A (AG = lower(AE)) from the value in registers
               if (GRAD) aG[u][d] = {lower<TG>(ae.re), lower<TG>(ae.im)};
             }
@@ -448,14 +477,14 @@ __global__ void __launch_bounds__(NT, COMP ? comp_min_blocks<K>() : ef_min_block
             }
           }
         }
+        if constexpr (!COMP) {
 #pragma unroll
-        for (int u = 0; u < IU; ++u)
-          if (P[u] > 0) {
-            if constexpr (COMP) eacc = eacc + df{re_mul<TL>(bar[u], H[u]), 0.0f};
-            else eacc = eacc + re_mul<TE>(bar[u], H[u]);
-          }
+          for (int u = 0; u < IU; ++u)
+            if (P[u] > 0) eacc = eacc + re_mul<TE>(bar[u], H[u]);
+        }
         if (GRAD) {
 #if EF_ITEM_RUNS
+          float eterm = 0.0f;  // compensated form: this iteration's energy terms
 #pragma unroll
           for (int u = 0; u < IU; ++u) {
             if (P[u] > 0) {
@@ -483,6 +512,15 @@ __global__ void __launch_bounds__(NT, COMP ? comp_min_blocks<K>() : ef_min_block
                 W[d].re += leaf ? h.re : TG(0);
                 W[d].im += leaf ? h.im : TG(0);
               }
+              if constexpr (COMP) {
+                // the item's prefix product is the path product at its depth
+                // (a term per depth, kept by a select: no indexed access)
+#pragma unroll
+                for (int d = 0; d < KP; ++d) {
+                  const float t = re_mul<TG>(Q[d], h);
+                  eterm += (d == cP - 1) ? t : 0.0f;
+                }
+              }
               // only full-length prefixes carry leaves
               const cpx<TG> bG = Q[KP - 1];
 #pragma unroll
@@ -493,6 +531,7 @@ __global__ void __launch_bounds__(NT, COMP ? comp_min_blocks<K>() : ef_min_block
                 }
             }
           }
+          if constexpr (COMP) eacc = eacc + df{eterm, 0.0f};
 #else
           cpx<TG> v[IU][KP];
 #pragma unroll
@@ -558,6 +597,10 @@ __global__ void __launch_bounds__(NT, COMP ? comp_min_blocks<K>() : ef_min_block
       if (tid == 0) a.E[e] = a.c0 + esum;
     }
     if (!GRAD) continue;
+    // every thread's item loop has written its private bins and atomics
+    // (without the energy's block sum above, the compensated form needs
+    // this barrier of its own)
+    if constexpr (COMP) __syncthreads();
     // private bins -> D (one warp per bin, lanes over threads)
     {
       const int lane = tid & 31, w = tid >> 5;
@@ -578,10 +621,11 @@ __global__ void __launch_bounds__(NT, COMP ? comp_min_blocks<K>() : ef_min_block
     }
     if constexpr (COMP) {
       // first-order correction for the FP32 rounding of A: Re sum_i D_i A_lo_i
+      const cpx<float> *Alo = (const cpx<float> *)AE + a.nA;
       for (int i = tid; i < a.nA; i += NT) {
-        const cpx<TE> ae = AE[i];
+        const cpx<float> lo = Alo[i];
         const cpx<TG> d = D[i];
-        eloc += (double)d.re * (double)Arith<TE>::lo(ae.re) - (double)d.im * (double)Arith<TE>::lo(ae.im);
+        eloc += (double)d.re * (double)lo.re - (double)d.im * (double)lo.im;
       }
       const double esum = block_sum(eloc, red);
       if (tid == 0) a.E[e] = a.c0 + esum;

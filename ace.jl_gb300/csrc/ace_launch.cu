@@ -99,6 +99,10 @@ int kernels_prepare(ace_ctx *ctx) {
     return ACE_ERR_UNSUPPORTED;
   }
   ctx->smem = lay.total;
+  // the compensated kernel's A_hi / A_lo arrays take the place of the
+  // double-float A and its FP32 copy: a smaller layout of its own
+  ctx->smem_comp = ef_layout(ctx->ntab, nRs, ctx->L, ctx->nA, ctx->chunkE, ctx->chunkG, ctx->npriv, NT, sE, sG, same,
+                             radj, true).total;
   int occ = 1;
   for (int g = 0; g < 3; ++g) {
     if (g == 2 && !uses_comp(ctx)) break;
@@ -108,7 +112,8 @@ int kernels_prepare(ace_ctx *ctx) {
       return ACE_ERR_CUDA;
     }
     // the grid follows the occupancy of the kernel the context's E+F calls run
-    if (g == (uses_comp(ctx) ? 2 : 1)) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, f, NT, lay.total);
+    if (g == (uses_comp(ctx) ? 2 : 1))
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, f, NT, g == 2 ? ctx->smem_comp : lay.total);
   }
   ctx->grid = ctx->nsm * std::max(occ, 1);
   // basis path (AA materialisation)
@@ -148,10 +153,12 @@ int launch_energy_forces(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const d
   EFArgs a = make_args(ctx, nEnv, off, rr, sp, E, G);
   if (ic) { a.ic = ic; a.c0 = c0; }
   void *f = ef_func(ctx, G != nullptr);
+  size_t smem = ctx->smem;
   if (!ic && !cpx && uses_comp(ctx)) {
     // energies with or without gradients: the correction needs the adjoint
     f = ef_func_comp(ctx);
     a.ic = ctx->d_ic32;
+    smem = ctx->smem_comp;
   }
   if (cpx) {
     f = ef_func_cplx(ctx, G != nullptr);
@@ -162,7 +169,7 @@ int launch_energy_forces(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const d
   }
   const int grid = (int)std::min<int64_t>(nEnv, ctx->grid);
   void *args[] = {&a};
-  cudaError_t e = cudaLaunchKernel(f, dim3(grid), dim3(NT), args, ctx->smem, st);
+  cudaError_t e = cudaLaunchKernel(f, dim3(grid), dim3(NT), args, smem, st);
   ctx->launches += 1;
   if (e != cudaSuccess) { ctx->err = cudaGetErrorString(e); return ACE_ERR_CUDA; }
   return ACE_OK;

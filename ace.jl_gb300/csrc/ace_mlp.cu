@@ -390,7 +390,7 @@ __global__ void adam_kernel(int64_t n, float *w, const float *g, float *m, float
 // K * 16 B between 8-row groups.
 
 constexpr uint32_t TC_COLS = 256;        // TMEM columns per CTA: values at 0, tangents at 128
-constexpr int TC_N3 = 96;                // output channels padded to a multiple of 16
+constexpr int TC_N3 = 128;               // output channels padded to a multiple of 16 (K (L+1) <= 128)
 constexpr int TC_K1 = 16;                // layer-1 inputs padded to one MMA K step
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }

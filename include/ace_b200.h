@@ -236,7 +236,7 @@ int ace_radial_mlp_forward(ace_ctx *ctx, int64_t nNbr, const double *rr, const i
 
 /* The radials the evaluation calls use (R and dR/dr as above): on GB300 a
    tensor-core kernel (tcgen05.mma, BF16 operands, FP32 accumulation) when
-   Q + nspecies <= 16 and K (L+1) <= 96, else the FP32 kernel;
+   Q + nspecies <= 16 and K (L+1) <= 128, else the FP32 kernel;
    ACE_B200_MLP=fp32 in the environment at ace_set_radial_mlp keeps FP32.
    ace_energy_radial_adjoint (training) always uses the FP32 MLP. */
 int ace_radial_mlp_infer(ace_ctx *ctx, int64_t nNbr, const double *rr, const int32_t *species, float *R,

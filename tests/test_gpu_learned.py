@@ -9,7 +9,12 @@
   (dE/drr, dE/dR);
 * one Adam step against its formula;
 * distillation from a plain 3-species model: the trained network beats the
-  same student before training (the species-blind polynomial radials);
+  same student before training and the method without the network (the
+  student spec's species-blind polynomial radials, coefficients fitted the
+  same way);
+* the force-loss gradient (a Hessian-vector product formed from two exact
+  energy gradients) against central differences of the force loss in the
+  MLP parameters: 3e-2 relative;
 * the plain-model fallback for environments outside the training radii.
 """
 import numpy as np
@@ -17,7 +22,7 @@ import pytest
 
 from ace_gb300.configs import random_batch
 from ace_gb300.learned import (LearnedRadialModel, RadialMLP, distill, energy_error, fit_coefficients,
-                               learned_context, pretrain_radial, student_spec)
+                               force_loss_gradient, learned_context, pretrain_radial, student_spec)
 from ace_gb300.spec import random_coefficients, symmetric_basis
 
 pytestmark = pytest.mark.gpu
@@ -165,8 +170,16 @@ def test_distillation_gain_and_fallback(lib):
     c1, hist = distill(ctx, mlp, spec, train, Etr, c0, steps=600, batch_envs=256, lr=2e-3, refit_every=200,
                        refit_envs=3000)
     err1 = energy_error(ctx.energy_forces(test.offsets, test.rr, test.species)[0], Ete)
-    print("untrained", err0, "trained", err1, "loss", hist[0], hist[-1])
+    # the method without the network: the student spec's own polynomial
+    # radials (species-blind, width K), coefficients fitted the same way
+    plain = lib.Context(spec, "fp32")
+    cp = fit_coefficients(plain, spec, train, Etr)
+    plain.set_params(cp)
+    err_plain = energy_error(plain.energy_forces(test.offsets, test.rr, test.species)[0], Ete)
+    plain.close()
+    print("untrained", err0, "trained", err1, "without network", err_plain, "loss", hist[0], hist[-1])
     assert err1["rel_rmse"] < 0.8 * err0["rel_rmse"]
+    assert err1["rel_rmse"] < 0.8 * err_plain["rel_rmse"]
     # fallback: an environment with a neighbour inside the training radii's
     # lower bound goes to the plain model, whose energy it reproduces exactly
     model = LearnedRadialModel(spec, mlp, c1, teacher, r_envelope=(0.8, 5.0))
@@ -199,3 +212,40 @@ def test_learned_basis_and_derivative(lib, oracle_mod, student, monkeypatch):
     Bref, dBref = orc.basis_d(b.offsets, b.rr, b.species)
     assert relerr(B, Bref) <= 1e-5
     assert relerr(dB, dBref) <= 1e-4
+
+
+def test_force_loss_gradient(lib, student):
+    torch = _torch()
+    spec, mlp = student
+    ctx = learned_context(spec, mlp, precision="fp64")
+    ctx.set_params(random_coefficients(spec, seed=5))
+    b = random_batch(8, 8, 20, nspecies=NS, seed=21)
+    dev = torch.device("cuda", 0)
+    off = torch.from_numpy(b.offsets).to(dev)
+    rr = torch.from_numpy(b.rr).to(dev)
+    sp = torch.from_numpy(b.species).to(dev)
+    E = torch.empty(b.nenv, dtype=torch.float64, device=dev)
+    G = torch.empty_like(rr)
+    GR = torch.empty((b.nnbr, mlp.C), dtype=torch.float32, device=dev)
+    ctx.energy_radial_adjoint(off, rr, sp, E, G, GR)
+    rng = np.random.default_rng(22)
+    Gt = G + 0.3 * float(G.abs().mean()) * torch.from_numpy(rng.standard_normal((b.nnbr, 3))).to(dev)
+    g = torch.zeros(len(mlp.params), dtype=torch.float32, device=dev)
+    loss = force_loss_gradient(ctx, g, off, rr, sp, G, Gt, 1.0, E, GR)
+    torch.cuda.synchronize()
+    g = g.cpu().numpy()
+
+    def loss_at(params):
+        ctx.set_radial_mlp(params, mlp.K, mlp.Q, mlp.nspecies, mlp.tmax)
+        _, Gp = ctx.energy_forces(b.offsets, b.rr, b.species)
+        Gth = Gt.cpu().numpy()
+        return float(np.mean((Gp - Gth) ** 2) / np.mean(Gth ** 2))
+    assert abs(loss_at(mlp.params) - loss) <= 1e-6 * loss
+    for k in np.argsort(-np.abs(g))[:4]:
+        d = 2e-3
+        p1, p0 = mlp.params.copy(), mlp.params.copy()
+        p1[k] += d
+        p0[k] -= d
+        num = (loss_at(p1) - loss_at(p0)) / (2 * d)
+        assert abs(num - g[k]) <= 3e-2 * abs(num), (k, num, g[k])
+    ctx.close()
