@@ -213,7 +213,8 @@ extern "C" int ace_ctx_create(const ace_spec_bundle *s, int32_t prec, int32_t de
     const size_t csz = (prec == ACE_PREC_FP64) ? 8 : (prec == ACE_PREC_FP32X2 ? 8 : 4);
     // item schedule
     const char *kenv = getenv("ACE_B200_KERNEL");
-    ctx->use_items = !(kenv && std::string(kenv) == "trie");
+    // (the compensated form exists on the item family of schedules only)
+    ctx->use_items = comp || !(kenv && std::string(kenv) == "trie");
     ItemSchedule its = build_items(sch, ctx->nt);
     ctx->item_n = its.n;
     ctx->ik.assign((size_t)(ITEM_G + 1) * its.n, -1);
@@ -238,6 +239,34 @@ extern "C" int ace_ctx_create(const ace_spec_bundle *s, int32_t prec, int32_t de
     if (cudaMemset(ctx->d_ic, 0, ctx->ik.size() * csz) != cudaSuccess) {
       g_create_error = "cudaMemset failed";
       return fail(ACE_ERR_CUDA);
+    }
+    // task schedule (orders >= 3)
+    if (s->maxord >= 3 && ctx->nt == 128) {
+      TaskSchedule ts = build_tasks(sch, ctx->nt / 32);
+      ctx->has_tasks = ctx->use_tasks = ts.rows > 0;
+      ctx->trows = ts.rows;
+      for (int w = 0; w <= ts.nwarps && w < 5; ++w) ctx->twrow[w] = ts.wrow[w];
+      ctx->tk = std::move(ts.ck);
+      ctx->tw = std::move(ts.cw);
+      if (ctx->has_tasks) {
+        if ((rc = upload(ctx, (uint16_t **)&ctx->d_trec, ts.rec.data(), ts.rec.size()))) {
+          g_create_error = ctx->err;
+          return fail(rc);
+        }
+        const size_t tsz = comp ? 4 : csz;
+        void **dst = comp ? (void **)&ctx->d_tc32 : &ctx->d_tc;
+        if (cudaMalloc(dst, ctx->tk.size() * tsz) != cudaSuccess) {
+          g_create_error = "cudaMalloc failed";
+          return fail(ACE_ERR_ALLOC);
+        }
+        ctx->allocs.push_back(*dst);
+        if (cudaMemset(*dst, 0, ctx->tk.size() * tsz) != cudaSuccess) {
+          g_create_error = "cudaMemset failed";
+          return fail(ACE_ERR_CUDA);
+        }
+      }
+      if (const char *kenv2 = getenv("ACE_B200_KERNEL"))
+        if (std::string(kenv2) == "items" || std::string(kenv2) == "trie") ctx->use_tasks = false;
     }
     if (comp) {
       if (cudaMalloc((void **)&ctx->d_ic32, ctx->ik.size() * sizeof(float)) != cudaSuccess) {
@@ -379,6 +408,17 @@ static int push_ctilde(ace_ctx *ctx) {
     std::vector<float> c(ctx->ik.size());
     for (size_t j = 0; j < c.size(); ++j) c[j] = ctx->ik[j] < 0 ? 0.f : (float)(ctx->iw[j] * ctx->ctilde[ctx->ik[j]]);
     ACE_CUDA(cudaMemcpy(ctx->d_ic32, c.data(), c.size() * sizeof(float), cudaMemcpyHostToDevice));
+  }
+  if (ctx->has_tasks) {
+    auto tval = [&](int64_t j) { return ctx->tk[j] < 0 ? 0.0 : ctx->tw[j] * ctx->ctilde[ctx->tk[j]]; };
+    if (ctx->comp) {
+      std::vector<float> c(ctx->tk.size());
+      for (size_t j = 0; j < c.size(); ++j) c[j] = (float)tval((int64_t)j);
+      ACE_CUDA(cudaMemcpy(ctx->d_tc32, c.data(), c.size() * sizeof(float), cudaMemcpyHostToDevice));
+    } else {
+      rc = pack_coefs(ctx, ctx->d_tc, (int64_t)ctx->tk.size(), tval);
+      if (rc) return rc;
+    }
   }
   const int64_t n = (int64_t)ctx->sslot.size();
   auto val = [&](int64_t j) { return ctx->sslot[j] < 0 ? 0.0 : ctx->sw[j] * ctx->ctilde[ctx->sslot[j]]; };
@@ -855,20 +895,23 @@ extern "C" int ace_autotune(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, 
   ACE_CUDA(cudaSetDevice(ctx->device));
   cudaStream_t st = (cudaStream_t)stream;
   const int regions[] = {16, 24, 32, 40, 48, 64};
-  // the compensated form exists for the item schedule only
-  const bool variants[] = {true, false};
-  const int nvariants = ctx->comp ? 1 : 2;
+  // candidates: the task schedule (orders >= 3), the item runs and, except
+  // for the compensated form (item family only), the trie walk
+  const int variants[] = {2, 1, 0};
+  const int nvariants = ctx->comp ? 2 : 3;
   float best = 1e30f;
   int best_region = ctx->region_kb;
-  bool best_items = ctx->use_items;
+  int best_variant = ctx->use_tasks ? 2 : ctx->use_items ? 1 : 0;
   cudaEvent_t e0, e1;
   ACE_CUDA(cudaEventCreate(&e0));
   ACE_CUDA(cudaEventCreate(&e1));
   reps = std::max(1, std::min(reps, 20));
   for (int vi = 0; vi < nvariants; ++vi) {
-    const bool items = variants[vi];
+    const int variant = variants[vi];
+    if (variant == 2 && !ctx->has_tasks) continue;
     for (int reg : regions) {
-      ctx->use_items = items;
+      ctx->use_tasks = variant == 2;
+      ctx->use_items = variant >= 1;
       ctx->region_kb = reg;
       if (kernels_prepare(ctx) != ACE_OK) continue;
       const int32_t *sp = input_species(ctx) > 1 ? species : nullptr;
@@ -881,16 +924,17 @@ extern "C" int ace_autotune(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, 
       timed = timed && cudaEventRecord(e1, st) == cudaSuccess && cudaEventSynchronize(e1) == cudaSuccess;
       float ms = 0.f;
       timed = timed && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess;
-      if (timed && cudaGetLastError() == cudaSuccess && ms < best) { best = ms; best_region = reg; best_items = items; }
+      if (timed && cudaGetLastError() == cudaSuccess && ms < best) { best = ms; best_region = reg; best_variant = variant; }
     }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  ctx->use_items = best_items;
+  ctx->use_tasks = best_variant == 2;
+  ctx->use_items = best_variant >= 1;
   ctx->region_kb = best_region;
   int rc = kernels_prepare(ctx);
   if (rc) return rc;
-  if (choice) *choice = best_region + (best_items ? 1000 : 0);
+  if (choice) *choice = best_region + 1000 * best_variant;
   return read_status(ctx, st);
 }
 

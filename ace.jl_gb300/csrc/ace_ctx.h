@@ -50,6 +50,16 @@ struct ace_ctx {
   std::vector<uint8_t> sw;     // slot -> weight
   // item schedule (ace_sched.h build_items)
   bool use_items = true;
+  // task schedule (ace_sched.h build_tasks; orders >= 3): the default
+  // correlation walk of single-property energy/force calls
+  bool has_tasks = false, use_tasks = false;
+  int64_t trows = 0;
+  int32_t twrow[5] = {0, 0, 0, 0, 0};
+  uint4 *d_trec = nullptr;
+  void *d_tc = nullptr;        // [rows * (G+1) * 32] coefficients in the energy type
+  float *d_tc32 = nullptr;     // the same in FP32 (compensated form)
+  std::vector<int64_t> tk;     // AA index of each task-schedule coefficient (-1: none)
+  std::vector<uint8_t> tw;     // weights
   // compensated form (ACE_PREC_FP32_COMP): prec is ACE_PREC_FP32X2 for every
   // other path; the single-property item kernel reads FP32 coefficients d_ic32
   bool comp = false;
@@ -135,6 +145,8 @@ int launch_energy_forces(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const d
 void *ef_func_cplx(const ace_ctx *ctx, bool grad);
 // compensated-form energy/force kernels (ace_launch_comp.cu)
 void *ef_func_comp(const ace_ctx *ctx);
+// task-schedule energy/force kernels (ace_launch_tasks.cu)
+void *ef_func_tasks(const ace_ctx *ctx, bool grad);
 int launch_basis(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const double *rr,
                  const int32_t *sp, double *B, double *dB, cudaStream_t st);
 int launch_dbasis(ace_ctx *ctx, int64_t nEnv, const int64_t *off_d, const int64_t *off_h, const double *rr,

@@ -79,6 +79,11 @@ struct EFArgs {
   int64_t in;
   double c0;
   int chunkE, chunkG, npriv;
+  // task schedule (ace_sched.h build_tasks): records, (G+1) coefficient rows
+  // per record row, and each warp's rows [twrow[w], twrow[w+1])
+  const uint4 *trec;
+  const void *tc;
+  int32_t twrow[5];
   int *status;
   // aa_kernel output
   void *AAout;
@@ -268,11 +273,15 @@ template <typename TE, int K> constexpr int ef_min_blocks() {
 // resident CTAs per SM of the compensated form: FP32 item state plus the
 // double-float A build and energy accumulator (no spills at orders 2-5)
 template <int K> constexpr int comp_min_blocks() { return EF_MIN_BLOCKS > 0 ? EF_MIN_BLOCKS : K <= 4 ? 6 : K == 5 ? 5 : 4; }
-template <typename TE, typename TG, int K, int NT, bool GRAD, bool ITEMS, bool CPX = false, bool COMP = false>
+// TASKS (item family, orders >= 3, NT = 128): the correlation phase walks the
+// task schedule (ace_sched.h build_tasks) instead of the per-thread item runs.
+template <typename TE, typename TG, int K, int NT, bool GRAD, bool ITEMS, bool CPX = false, bool COMP = false,
+          bool TASKS = false>
 __global__ void __launch_bounds__(NT, COMP ? comp_min_blocks<K>() : ef_min_blocks<TE, CPX ? K + 1 : K>())
     ef_kernel(EFArgs a) {
   static_assert(ITEMS || !CPX, "complex coefficients need the item schedule");
-  static_assert(!COMP || (ITEMS && GRAD && !CPX && EF_ITEM_RUNS && std::is_same<TE, df>::value &&
+  static_assert(!TASKS || (ITEMS && !CPX && K >= 3 && NT == 128), "the task schedule: real coefficients, K >= 3");
+  static_assert(!COMP || (ITEMS && GRAD && !CPX && (EF_ITEM_RUNS || TASKS) && std::is_same<TE, df>::value &&
                           std::is_same<TG, float>::value),
                 "the compensated form is the double-float A with FP32 item products and the run adjoint");
   constexpr bool SAME = std::is_same<TE, TG>::value;
@@ -395,6 +404,126 @@ __global__ void __launch_bounds__(NT, COMP ? comp_min_blocks<K>() : ef_min_block
     for (int d = K; d >= 1; --d)
       if (d <= cur) close(d);
       eacc = H[0].re;
+    } else if constexpr (TASKS) {
+      // Each warp runs its rows of the task schedule; a row is uniform
+      // across the warp (one type, one item count), so the lanes run their
+      // tasks in lockstep.  Per task: Q_t = prod A_t; per item Q = Q_t A_mid,
+      // the energy Re(Q H), H = c_own + sum_g c_g A_leaf_g, and the
+      // adjoints D[leaf_g] += Q c_g, D[mid] += H Q_t, W += H A_mid; at the
+      // end D[t_d] += W prod_{d' != d} A_t_d'.  Short items: the flat
+      // product and its local adjoints.
+      constexpr int KT = (K >= 3) ? K - 2 : 1;
+      constexpr int G1 = ITEM_G + 1;
+      constexpr bool ONE = std::is_same<TL, TG>::value;  // products and adjoint in one type
+      const int lane = tid & 31, wp = tid >> 5;
+      const cpx<TG> gone = {TG(1), TG(0)};
+      const TL ze = Arith<TL>::zero();
+      for (int64_t row = a.twrow[wp]; row < a.twrow[wp + 1];) {
+        const uint4 hr = __ldg(a.trec + row * 32 + lane);
+        const int type = (int)(hr.w >> 16), n = (int)(hr.w & 0xffffu);
+        const uint32_t hw[2] = {hr.x, hr.y};
+        if (type == 1) {
+          int t[KT];
+          cpx<TG> ag[KT];
+          cpx<TL> QtL = {Arith<TL>::one(), ze};
+#pragma unroll
+          for (int d = 0; d < KT; ++d) {
+            t[d] = (int)((hw[d >> 1] >> (16 * (d & 1))) & 0xffffu);
+            const cpx<TL> av = AL[t[d]];
+            QtL = (d == 0) ? av : cmul(QtL, av);
+            ag[d] = {lower<TG>(av.re), lower<TG>(av.im)};
+          }
+          cpx<TG> QtG = gone;
+          if constexpr (ONE) {
+            QtG = {lower<TG>(QtL.re), lower<TG>(QtL.im)};
+          } else {
+#pragma unroll
+            for (int d = 0; d < KT; ++d) QtG = (d == 0) ? ag[d] : cmul(QtG, ag[d]);
+          }
+          cpx<TG> Wt = {TG(0), TG(0)};
+          float eterm = 0.0f;  // compensated form: the task's energy terms
+#pragma unroll 2
+          for (int j = 0; j < n; ++j) {
+            const int64_t ir = row + 1 + j;
+            const uint4 rc = __ldg(a.trec + ir * 32 + lane);
+            const int mid = (int)(rc.x & 0xffffu), nl = (int)(rc.w & 0xffffu);
+            const int lf[2] = {(int)(rc.x >> 16), (int)(rc.y & 0xffffu)};
+            const int64_t cb = ir * (G1 * 32) + lane;
+            cpx<TL> H = {load_coef<TL>(a.tc, cb), ze};
+            TL cg[ITEM_G];
+#pragma unroll
+            for (int g = 0; g < ITEM_G; ++g) {
+              cg[g] = load_coef<TL>(a.tc, cb + (g + 1) * 32);
+              if (g < nl) H = cfma(H, AL[lf[g < 2 ? g : 0]], cg[g]);
+            }
+            const cpx<TL> am = AL[mid];
+            const cpx<TL> QL = cmul(QtL, am);
+            if constexpr (COMP) eterm += re_mul<TL>(QL, H);
+            else eacc = eacc + re_mul<TE>(QL, H);
+            if (GRAD) {
+              const cpx<TG> amg = {lower<TG>(am.re), lower<TG>(am.im)};
+              cpx<TG> QG;
+              if constexpr (ONE) QG = {lower<TG>(QL.re), lower<TG>(QL.im)};
+              else QG = cmul(QtG, amg);
+              const cpx<TG> h = {lower<TG>(H.re), lower<TG>(H.im)};
+#pragma unroll
+              for (int g = 0; g < ITEM_G; ++g)
+                if (g < nl) dacc(lf[g < 2 ? g : 0], cscale(QG, lower<TG>(cg[g])));
+              dacc(mid, cmul(h, QtG));
+              Wt = cadd(Wt, cmul(h, amg));
+            }
+          }
+          if constexpr (COMP) eacc = eacc + df{eterm, 0.0f};
+          if (GRAD) {
+            // W over the task prefix: prefix and suffix products
+            cpx<TG> pre = gone;
+#pragma unroll
+            for (int d = 0; d < KT; ++d) {
+              cpx<TG> suf = gone;
+#pragma unroll
+              for (int e = d + 1; e < KT; ++e) suf = (e == d + 1) ? ag[e] : cmul(suf, ag[e]);
+              dacc(t[d], cmul(Wt, cmul(pre, suf)));
+              pre = (d == 0) ? ag[0] : cmul(pre, ag[d]);
+            }
+          }
+          row += 1 + n;
+        } else {
+          // short item: P = n < K - 1 indices in [0..P)
+          const int P = n;
+          const TL c = load_coef<TL>(a.tc, row * (G1 * 32) + lane);
+          int v[KT];
+          cpx<TG> ag[KT];
+          cpx<TL> p = {Arith<TL>::one(), ze};
+#pragma unroll
+          for (int d = 0; d < KT; ++d) {
+            v[d] = (int)((hw[d >> 1] >> (16 * (d & 1))) & 0xffffu);
+            ag[d] = gone;
+            if (d < P) {
+              const cpx<TL> av = AL[v[d]];
+              p = (d == 0) ? av : cmul(p, av);
+              ag[d] = {lower<TG>(av.re), lower<TG>(av.im)};
+            }
+          }
+          if constexpr (COMP) eacc = eacc + df{c * p.re, 0.0f};
+          else eacc = eacc + c * p.re;
+          if (GRAD) {
+            const TG cG = lower<TG>(c);
+            cpx<TG> pre = gone;
+#pragma unroll
+            for (int d = 0; d < KT; ++d) {
+              if (d < P) {
+                cpx<TG> suf = gone;
+#pragma unroll
+                for (int e = d + 1; e < KT; ++e)
+                  if (e < P) suf = cmul(suf, ag[e]);
+                dacc(v[d], cscale(cmul(pre, suf), cG));
+                pre = cmul(pre, ag[d]);
+              }
+            }
+          }
+          row += 1;
+        }
+      }
     } else {
       // EF_ITEM_ILP items per thread and iteration, interleaved: their
       // product chains and warp reductions are independent, which hides the
@@ -855,6 +984,8 @@ inline EFArgs make_args(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const do
   a.irec = ctx->d_irec; a.ic = ctx->d_ic; a.in = ctx->item_n;
   a.c0 = ctx->has_const ? ctx->ctilde[0] : 0.0;
   a.chunkE = ctx->chunkE; a.chunkG = ctx->chunkG; a.npriv = ctx->npriv;
+  a.trec = ctx->d_trec; a.tc = ctx->d_tc;
+  for (int w = 0; w < 5; ++w) a.twrow[w] = ctx->twrow[w];
   a.status = ctx->d_status;
   a.ord = ctx->d_ord; a.idx = ctx->d_idx; a.nAA = ctx->nAA;
   return a;

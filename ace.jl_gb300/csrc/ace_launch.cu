@@ -2,6 +2,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <vector>
 
 #include "../../include/ace_b200.h"
 #include "ace_ctx.h"
@@ -56,6 +57,25 @@ static void *ub_func(const ace_ctx *ctx) {
 // the compensated kernels replace the double-float item kernels for the
 // single-property energy/force calls of a compensated context
 static bool uses_comp(const ace_ctx *ctx) { return ctx->comp && ctx->use_items && !ctx->learned; }
+// single-property energy/force calls walk the task schedule (orders >= 3)
+static bool uses_tasks(const ace_ctx *ctx) { return ctx->has_tasks && ctx->use_tasks && !ctx->learned; }
+
+// the kernel a context's single-property energy/force calls launch, its
+// coefficient array and its shared-memory size
+static void *ef_main(const ace_ctx *ctx, bool grad, const void **coef, size_t *smem) {
+  const bool comp = uses_comp(ctx);
+  *smem = comp ? ctx->smem_comp : ctx->smem;
+  if (uses_tasks(ctx)) {
+    *coef = comp ? (const void *)ctx->d_tc32 : ctx->d_tc;
+    return ef_func_tasks(ctx, grad);
+  }
+  if (comp) {
+    *coef = ctx->d_ic32;
+    return ef_func_comp(ctx);
+  }
+  *coef = ctx->d_ic;
+  return ef_func(ctx, grad);
+}
 
 static void type_sizes(const ace_ctx *ctx, int &sE, int &sG, bool &same) {
   switch (ctx->prec) {
@@ -104,16 +124,20 @@ int kernels_prepare(ace_ctx *ctx) {
   ctx->smem_comp = ef_layout(ctx->ntab, nRs, ctx->L, ctx->nA, ctx->chunkE, ctx->chunkG, ctx->npriv, NT, sE, sG, same,
                              radj, true).total;
   int occ = 1;
-  for (int g = 0; g < 3; ++g) {
-    if (g == 2 && !uses_comp(ctx)) break;
-    void *f = g == 2 ? ef_func_comp(ctx) : ef_func(ctx, g == 1);
+  std::vector<void *> fs = {ef_func(ctx, false), ef_func(ctx, true)};
+  if (uses_comp(ctx)) fs.push_back(ef_func_comp(ctx));
+  if (ctx->has_tasks) { fs.push_back(ef_func_tasks(ctx, false)); fs.push_back(ef_func_tasks(ctx, true)); }
+  for (void *f : fs)
     if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, ctx->smem_optin) != cudaSuccess) {
       ctx->err = "cudaFuncSetAttribute failed";
       return ACE_ERR_CUDA;
     }
+  {
     // the grid follows the occupancy of the kernel the context's E+F calls run
-    if (g == (uses_comp(ctx) ? 2 : 1))
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, f, NT, g == 2 ? ctx->smem_comp : lay.total);
+    const void *coef;
+    size_t sm;
+    void *f = ef_main(ctx, true, &coef, &sm);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, f, NT, sm);
   }
   ctx->grid = ctx->nsm * std::max(occ, 1);
   // basis path (AA materialisation)
@@ -154,11 +178,13 @@ int launch_energy_forces(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const d
   if (ic) { a.ic = ic; a.c0 = c0; }
   void *f = ef_func(ctx, G != nullptr);
   size_t smem = ctx->smem;
-  if (!ic && !cpx && uses_comp(ctx)) {
-    // energies with or without gradients: the correction needs the adjoint
-    f = ef_func_comp(ctx);
-    a.ic = ctx->d_ic32;
-    smem = ctx->smem_comp;
+  if (!ic && !cpx) {
+    // the single-property kernel: task schedule, compensated form (whose
+    // energies need the adjoint, with or without gradients) or item runs
+    const void *coef;
+    f = ef_main(ctx, G != nullptr, &coef, &smem);
+    if (uses_tasks(ctx)) a.tc = coef;
+    else a.ic = coef;
   }
   if (cpx) {
     f = ef_func_cplx(ctx, G != nullptr);

@@ -390,6 +390,212 @@ inline ItemSchedule build_items(const Schedule &s, int nthreads) {
   return it;
 }
 
+// ----------------------------------------------------------------------------
+// Task schedule (orders K >= 3).  A task is a node of the prefix trie at depth
+// KT - 1 (KT = K - 2): a prefix t = (v1..v_KT) and the full-length items
+// below it, each item one more prefix index ("mid", v_{KT+1}), up to G
+// leaves and the coefficient of the prefix function (t, mid) itself.  A lane
+// evaluates a whole task: the task product Q_t = prod A_t once, for every
+// item Q = Q_t A_mid, the energy Re(Q (c_own + sum_g c_g A_leaf_g)) and the
+// adjoints (leaves: Q c_g; mid: H Q_t; the task's W += H A_mid), and at the
+// end distributes W over the task prefix (D[t_d] += W prod_{d' != d} A_t_d').
+// The same sums as the trie walk (src/pibasis.jl:338-390, grouped by node),
+// with no open path carried from task to task.
+//
+// Tasks with the same item count are grouped 32 at a time into warp
+// "slots", so the lanes of a warp run tasks of equal length in lockstep (the
+// last slot of each count is padded with zero-coefficient tasks); functions
+// of order < K - 1 are "short" items, 32 of equal order per row, evaluated
+// flat (product and local adjoints).  Slots are assigned to the warps of the
+// CTA longest first, each to the warp with the fewest rows.
+//
+// Each warp runs its rows [wrow[w], wrow[w+1]); row r of lane l is record
+// r * 32 + l (16 bytes, 8 uint16): a task header (type 1: t in [0..KT), the
+// item count n in [6]), an item (type 2: mid in [0], leaves in [1..G],
+// nl in [6]) or a short item (type 3: its indices in [0..P), P in [6]);
+// [7] holds the type.  Coefficients: (1 + G) rows per record row,
+// coefficient g of row r, lane l at ((r (1 + G) + g) 32 + l): an item's own
+// coefficient and its leaves', a short item's in g = 0.
+static constexpr int TASK_LANES = 32;
+
+struct TaskSchedule {
+  int K = 0, KT = 0, nwarps = 0;
+  int64_t rows = 0;
+  std::vector<int32_t> wrow;       // [nwarps + 1]
+  std::vector<uint16_t> rec;       // [rows * 32 * 8]
+  std::vector<int64_t> ck;         // [rows * (1 + G) * 32] AA index of each coefficient (-1: none)
+  std::vector<uint8_t> cw;         // weights (1, or 2 for a conjugate pair)
+  int64_t tasks = 0, items = 0, shorts = 0, pad_items = 0;
+};
+
+inline TaskSchedule build_tasks(const Schedule &s, int nwarps) {
+  TaskSchedule ts;
+  const int K = s.K, KP = K - 1, KT = K - 2, G = ITEM_G;
+  ts.K = K;
+  ts.KT = KT;
+  ts.nwarps = nwarps;
+  if (K < 3) return ts;
+  auto vat = [&](int64_t i, int j) { return (int)s.v[(size_t)j * s.n + i]; };
+  struct It { int mid; int nl; int leaf[ITEM_G]; int64_t kown; uint8_t wown; int64_t kl[ITEM_G]; uint8_t wl[ITEM_G]; };
+  struct Task { int t[6]; std::vector<It> items; };
+  struct Short { int P; int v[6]; int64_t k; uint8_t w; };
+  std::vector<Task> tasks;
+  std::vector<Short> shorts;
+  // one pass in lexicographic order: the functions of a full prefix
+  // (t, mid) -- the prefix function first, then its extensions -- are
+  // adjacent, and so are the prefixes of a task
+  int cur[6] = {-1, -1, -1, -1, -1, -1};
+  bool have = false;
+  auto open_item = [&](int64_t i) {
+    bool same_task = have;
+    for (int j = 0; j < KT && same_task; ++j) same_task = tasks.back().t[j] == vat(i, j);
+    if (!same_task) {
+      Task t;
+      for (int j = 0; j < 6; ++j) t.t[j] = j < KT ? vat(i, j) : 0;
+      tasks.push_back(t);
+      have = true;
+      cur[KT] = -1;
+    }
+    Task &t = tasks.back();
+    const int mid = vat(i, KT);
+    if (t.items.empty() || cur[KT] != mid || t.items.back().nl == G) {
+      It x{};
+      x.mid = mid;
+      x.kown = -1;
+      for (int g = 0; g < G; ++g) x.kl[g] = -1;
+      // a repeated mid (more than G leaves) starts a new item without the
+      // prefix function's coefficient
+      t.items.push_back(x);
+      cur[KT] = mid;
+    }
+  };
+  for (int64_t i = 0; i < s.n; ++i) {
+    const int o = s.ord[i];
+    if (o == K) {
+      open_item(i);
+      It &x = tasks.back().items.back();
+      x.leaf[x.nl] = vat(i, KP);
+      x.kl[x.nl] = s.k[i];
+      x.wl[x.nl] = s.w[i];
+      ++x.nl;
+    } else if (o == KP) {
+      open_item(i);
+      It &x = tasks.back().items.back();
+      if (x.kown >= 0 || x.nl > 0) {  // (cannot happen in lexicographic order: the prefix sorts first)
+        It y{};
+        y.mid = x.mid;
+        for (int g = 0; g < G; ++g) y.kl[g] = -1;
+        tasks.back().items.push_back(y);
+      }
+      tasks.back().items.back().kown = s.k[i];
+      tasks.back().items.back().wown = s.w[i];
+    } else {
+      Short sh{};
+      sh.P = o;
+      for (int j = 0; j < o; ++j) sh.v[j] = vat(i, j);
+      sh.k = s.k[i];
+      sh.w = s.w[i];
+      shorts.push_back(sh);
+    }
+  }
+  ts.tasks = (int64_t)tasks.size();
+  ts.shorts = (int64_t)shorts.size();
+  // slots: 32 tasks of equal item count, or 32 short items of equal order
+  struct Slot { int kind; int n; std::vector<int> who; int64_t rows; };
+  std::vector<Slot> slots;
+  {
+    std::map<int, std::vector<int>> bycount;
+    for (int i = 0; i < (int)tasks.size(); ++i) bycount[(int)tasks[i].items.size()].push_back(i);
+    for (auto &kv : bycount)
+      for (size_t q = 0; q < kv.second.size(); q += TASK_LANES) {
+        Slot sl;
+        sl.kind = 1;
+        sl.n = kv.first;
+        for (size_t r = q; r < std::min(kv.second.size(), q + TASK_LANES); ++r) sl.who.push_back(kv.second[r]);
+        sl.rows = 1 + kv.first;
+        ts.items += (int64_t)sl.who.size() * kv.first;
+        ts.pad_items += (int64_t)(TASK_LANES - sl.who.size()) * kv.first;
+        slots.push_back(sl);
+      }
+    std::map<int, std::vector<int>> byord;
+    for (int i = 0; i < (int)shorts.size(); ++i) byord[shorts[i].P].push_back(i);
+    for (auto &kv : byord)
+      for (size_t q = 0; q < kv.second.size(); q += TASK_LANES) {
+        Slot sl;
+        sl.kind = 3;
+        sl.n = kv.first;
+        for (size_t r = q; r < std::min(kv.second.size(), q + TASK_LANES); ++r) sl.who.push_back(kv.second[r]);
+        sl.rows = 1;
+        slots.push_back(sl);
+      }
+  }
+  // balance: longest slots first, each to the warp with the fewest rows
+  std::vector<size_t> order(slots.size());
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) { return slots[x].rows > slots[y].rows; });
+  std::vector<std::vector<size_t>> own(nwarps);
+  std::vector<int64_t> load(nwarps, 0);
+  for (size_t si : order) {
+    int w = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+    own[w].push_back(si);
+    load[w] += slots[si].rows;
+  }
+  ts.wrow.assign(nwarps + 1, 0);
+  for (int w = 0; w < nwarps; ++w) ts.wrow[w + 1] = ts.wrow[w] + (int32_t)load[w];
+  ts.rows = ts.wrow[nwarps];
+  ts.rec.assign((size_t)ts.rows * TASK_LANES * 8, 0);
+  ts.ck.assign((size_t)ts.rows * (1 + G) * TASK_LANES, -1);
+  ts.cw.assign((size_t)ts.rows * (1 + G) * TASK_LANES, 0);
+  auto recp = [&](int64_t row, int lane) { return &ts.rec[((size_t)row * TASK_LANES + lane) * 8]; };
+  auto setc = [&](int64_t row, int g, int lane, int64_t k, uint8_t w) {
+    const size_t q = ((size_t)row * (1 + G) + g) * TASK_LANES + lane;
+    ts.ck[q] = k;
+    ts.cw[q] = w;
+  };
+  for (int w = 0; w < nwarps; ++w) {
+    int64_t row = ts.wrow[w];
+    for (size_t si : own[w]) {
+      const Slot &sl = slots[si];
+      if (sl.kind == 1) {
+        for (int lane = 0; lane < TASK_LANES; ++lane) {
+          uint16_t *h = recp(row, lane);
+          h[6] = (uint16_t)sl.n;
+          h[7] = 1;
+          for (int j = 0; j < sl.n; ++j) {
+            uint16_t *r = recp(row + 1 + j, lane);
+            r[6] = 0;
+            r[7] = 2;
+          }
+          if (lane >= (int)sl.who.size()) continue;  // padding: index 0, no coefficients
+          const Task &t = tasks[sl.who[lane]];
+          for (int d = 0; d < KT; ++d) h[d] = (uint16_t)t.t[d];
+          for (int j = 0; j < sl.n; ++j) {
+            const It &x = t.items[j];
+            uint16_t *r = recp(row + 1 + j, lane);
+            r[0] = (uint16_t)x.mid;
+            for (int g = 0; g < x.nl; ++g) r[1 + g] = (uint16_t)x.leaf[g];
+            r[6] = (uint16_t)x.nl;
+            if (x.kown >= 0) setc(row + 1 + j, 0, lane, x.kown, x.wown);
+            for (int g = 0; g < x.nl; ++g) setc(row + 1 + j, 1 + g, lane, x.kl[g], x.wl[g]);
+          }
+        }
+      } else {
+        for (int lane = 0; lane < TASK_LANES; ++lane) {
+          uint16_t *r = recp(row, lane);
+          r[6] = (uint16_t)sl.n;
+          r[7] = 3;
+          if (lane >= (int)sl.who.size()) continue;
+          const Short &sh = shorts[sl.who[lane]];
+          for (int d = 0; d < sh.P; ++d) r[d] = (uint16_t)sh.v[d];
+          setc(row, 0, lane, sh.k, sh.w);
+        }
+      }
+      row += sl.rows;
+    }
+  }
+  return ts;
+}
+
 // Fused symmetric-basis table (B = U real(AA) without AA in memory).  U's
 // rows are grouped into classes -- consecutive rows whose AA columns overlap
 // (the rows of one (n, l)-class; different classes use disjoint AA

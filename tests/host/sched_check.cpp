@@ -1,7 +1,7 @@
 // Host-logic check of the correlation schedules (ace_sched.h): evaluates the
-// energy and the adjoint dE/dA in double precision through (1) the trie walk
-// and (2) the item schedule with the per-warp segmented reductions, exactly as
-// the kernels order them, and compares with the flat products of the spec
+// energy and the adjoint dE/dA in double precision through (1) the trie walk,
+// (2) the item schedule and (3) the task schedule, exactly as the kernels
+// order them, and compares with the flat products of the spec
 // (src/evaluator.jl:121-147, src/pibasis.jl:338-390).  Inputs are binary
 // dumps written by tests/test_sched_host.py; prints one line of errors.
 #include <complex>
@@ -169,11 +169,72 @@ int main(int argc, char **argv) {
     }
   }
 #endif
+  // (3) tasks (orders >= 3): per warp, per lane, the rows of the warp's
+  // program as the kernel walks them
+  double Ek = ct[0];
+  std::vector<C> Dk(nA);
+  TaskSchedule ts = build_tasks(s, NT / 32);
+  if (K >= 3) {
+    const int KT = ts.KT, L = TASK_LANES;
+    auto coefk = [&](int64_t row, int g, int lane) {
+      const size_t q = ((size_t)row * (1 + G) + g) * L + lane;
+      return ts.ck[q] < 0 ? 0.0 : ts.cw[q] * ct[ts.ck[q]];
+    };
+    for (int w = 0; w < ts.nwarps; ++w)
+      for (int lane = 0; lane < L; ++lane)
+        for (int64_t row = ts.wrow[w]; row < ts.wrow[w + 1];) {
+          const uint16_t *h = &ts.rec[((size_t)row * L + lane) * 8];
+          if (h[7] == 1) {
+            const int n = h[6];
+            C Qt = 1, Wt = 0;
+            for (int d = 0; d < KT; ++d) Qt *= A[h[d]];
+            for (int j = 0; j < n; ++j) {
+              const int64_t ir = row + 1 + j;
+              const uint16_t *r = &ts.rec[((size_t)ir * L + lane) * 8];
+              if (r[7] != 2) { printf("bad-item-row\n"); return 1; }
+              const C am = A[r[0]];
+              C H = coefk(ir, 0, lane);
+              for (int g = 0; g < r[6]; ++g) H += coefk(ir, 1 + g, lane) * A[r[1 + g]];
+              const C Q = Qt * am;
+              Ek += (Q * H).real();
+              for (int g = 0; g < r[6]; ++g) Dk[r[1 + g]] += coefk(ir, 1 + g, lane) * Q;
+              Dk[r[0]] += H * Qt;
+              Wt += H * am;
+            }
+            for (int d = 0; d < KT; ++d) {
+              C p = Wt;
+              for (int e = 0; e < KT; ++e) if (e != d) p *= A[h[e]];
+              Dk[h[d]] += p;
+            }
+            row += 1 + n;
+          } else if (h[7] == 3) {
+            const int P = h[6];
+            const double c = coefk(row, 0, lane);
+            C p = 1;
+            for (int d = 0; d < P; ++d) p *= A[h[d]];
+            Ek += c * p.real();
+            for (int d = 0; d < P; ++d) {
+              C q = c;
+              for (int e = 0; e < P; ++e) if (e != d) q *= A[h[e]];
+              Dk[h[d]] += q;
+            }
+            row += 1;
+          } else {
+            printf("bad-row-type %d\n", h[7]);
+            return 1;
+          }
+        }
+  } else {
+    Ek = Eref;
+    Dk = Dref;
+  }
   // the kernels' adjoint is exact along conjugation-symmetric directions W
-  C gr = 0, gt = 0, gi = 0;
-  for (int i = 0; i < nA; ++i) { gr += Dref[i] * W[i]; gt += Dt[i] * W[i]; gi += Di[i] * W[i]; }
-  printf("%d %lld %lld %.3e %.3e %.3e %.3e\n", (int)s.halved, (long long)s.n, (long long)it.n,
+  C gr = 0, gt = 0, gi = 0, gk = 0;
+  for (int i = 0; i < nA; ++i) { gr += Dref[i] * W[i]; gt += Dt[i] * W[i]; gi += Di[i] * W[i]; gk += Dk[i] * W[i]; }
+  printf("%d %lld %lld %.3e %.3e %.3e %.3e %.3e %.3e %lld %lld\n", (int)s.halved, (long long)s.n, (long long)it.n,
          std::abs(Et - Eref) / std::abs(Eref), std::abs(Ei - Eref) / std::abs(Eref),
-         std::abs(gt.real() - gr.real()) / std::abs(gr.real()), std::abs(gi.real() - gr.real()) / std::abs(gr.real()));
+         std::abs(gt.real() - gr.real()) / std::abs(gr.real()), std::abs(gi.real() - gr.real()) / std::abs(gr.real()),
+         std::abs(Ek - Eref) / std::abs(Eref), std::abs(gk.real() - gr.real()) / std::abs(gr.real()),
+         (long long)ts.rows, (long long)ts.pad_items);
   return 0;
 }

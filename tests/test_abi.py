@@ -53,9 +53,10 @@ def test_header_compiles_as_c99(tmp_path):
 
 
 def test_energy_force_kernels_do_not_spill(tmp_path):
-    """The per-type register bounds of the energy/force kernel (ef_min_blocks)
-    leave the item-schedule instantiations of orders 2-5 without local-memory
-    spills (ptxas resource report; the code itself is not read)."""
+    """The per-type register bounds of the energy/force kernel (ef_min_blocks,
+    comp_min_blocks) leave the item-run and task-schedule instantiations of
+    orders 2-5 without local-memory spills (ptxas resource report; the code
+    itself is not read)."""
     import re
     import shutil
     import subprocess
@@ -63,7 +64,7 @@ def test_energy_force_kernels_do_not_spill(tmp_path):
     if not os.path.exists(nvcc):
         pytest.skip("nvcc not available")
     err = ""
-    for name in ("ace_launch.cu", "ace_launch_comp.cu"):
+    for name in ("ace_launch.cu", "ace_launch_comp.cu", "ace_launch_tasks.cu"):
         src = os.path.join(ROOT, "ace.jl_gb300", "csrc", name)
         r = subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "-Xptxas", "-v",
                             "-I", os.path.join(ROOT, "include"), "-c", src, "-o", str(tmp_path / "l.o")],
@@ -81,8 +82,10 @@ def test_energy_force_kernels_do_not_spill(tmp_path):
     dem = subprocess.run(["c++filt"], input="\n".join(names), capture_output=True, text=True).stdout.splitlines()
     checked = 0
     for mangled, d in zip(names, dem):
-        m = re.search(r"ef_kernel<(.+), (\d), 128, true, true, false, (false|true)>", d)
+        m = re.search(r"ef_kernel<(.+), (\d), 128, true, true, false, (false|true), (false|true)>", d)
         if m and 2 <= int(m.group(2)) <= 5:
             assert report[mangled] == 0, d
             checked += 1
-    assert checked == 16  # {float, double-float, double, compensated} x orders 2..5
+    # {float, double-float, double, compensated} x (item runs: orders 2..5,
+    # task schedule: orders 3..5)
+    assert checked == 28

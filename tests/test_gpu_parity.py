@@ -462,3 +462,22 @@ def test_contexts_of_different_sizes_interleave(lib, oracle_mod):
     Eb2, _ = cb.energy_forces(b.offsets, b.rr)        # after the smaller context's set-up
     Bb2 = cb.basis(b.offsets, b.rr)
     assert np.array_equal(Eb1, Eb2) and np.array_equal(Bb1, Bb2)
+
+
+@pytest.mark.parametrize("kernel", ["items", "trie"])
+@pytest.mark.parametrize("prec", ["fp64", "fp32", "fp32x2", "fp32c"])
+def test_other_schedules(lib, oracle_mod, prec, kernel, monkeypatch):
+    """The task schedule is the default correlation walk for orders >= 3;
+    the per-thread item runs and the trie walk (ACE_B200_KERNEL, read at
+    context creation) stay selectable and give the same results (the
+    compensated form has no trie walk and keeps its item runs)."""
+    monkeypatch.setenv("ACE_B200_KERNEL", kernel)
+    spec = get_spec("cfg2")
+    c = random_coefficients(spec, seed=11)
+    b = random_batch(100, 20, 60, seed=5)
+    Eref, Gref = oracle_mod.Oracle(spec, c).energy_forces(b.offsets, b.rr)
+    ctx = lib.Context(spec, prec)
+    ctx.set_params(c)
+    E, G = ctx.energy_forces(b.offsets, b.rr)
+    assert energy_relerr(E, Eref) <= TOL[prec]["E"]
+    assert relerr(G, Gref) <= TOL[prec]["G"]

@@ -1,5 +1,5 @@
 """Host logic of the correlation schedules (ace.jl_gb300/csrc/ace_sched.h):
-the trie walk and the item schedule with segmented warp reductions, replayed
+the trie walk, the item schedule and the task schedule, replayed
 in double precision by tests/host/sched_check.cpp, must reproduce the flat
 products of the reference evaluator (energy, and the adjoint along
 conjugation-symmetric directions, which is what the forces contract with)."""
@@ -56,7 +56,7 @@ def test_schedules_match_flat_products(checker, oracle_mod, tmp_path, args):
         np.ascontiguousarray(arr, dtype=dt).tofile(str(tmp_path / f"{name}.bin"))
     out = subprocess.run([checker, str(tmp_path)], capture_output=True, text=True, check=True).stdout.split()
     halved, n, nitems = int(out[0]), int(out[1]), int(out[2])
-    eT, eI, gT, gI = map(float, out[3:7])
+    eT, eI, gT, gI, eK, gK = map(float, out[3:9])
     assert halved == 1
-    assert eT < 1e-12 and eI < 1e-12
-    assert gT < 1e-11 and gI < 1e-11
+    assert eT < 1e-12 and eI < 1e-12 and eK < 1e-12
+    assert gT < 1e-11 and gI < 1e-11 and gK < 1e-11
