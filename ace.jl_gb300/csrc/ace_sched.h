@@ -402,9 +402,10 @@ inline ItemSchedule build_items(const Schedule &s, int nthreads) {
 // The same sums as the trie walk (src/pibasis.jl:338-390, grouped by node),
 // with no open path carried from task to task.
 //
-// Tasks with the same item count are grouped 32 at a time into warp
-// "slots", so the lanes of a warp run tasks of equal length in lockstep (the
-// last slot of each count is padded with zero-coefficient tasks); functions
+// Tasks sorted by item count are grouped 32 at a time into warp "slots", so
+// the lanes of a warp run tasks of (nearly) equal length in lockstep: a
+// slot's length is its longest task's, shorter tasks end in zero-coefficient
+// items, and the last slot is padded with zero-coefficient tasks; functions
 // of order < K - 1 are "short" items, 32 of equal order per row, evaluated
 // flat (product and local adjoints).  Slots are assigned to the warps of the
 // CTA longest first, each to the warp with the fewest rows.
@@ -504,19 +505,26 @@ inline TaskSchedule build_tasks(const Schedule &s, int nwarps) {
   struct Slot { int kind; int n; std::vector<int> who; int64_t rows; };
   std::vector<Slot> slots;
   {
-    std::map<int, std::vector<int>> bycount;
-    for (int i = 0; i < (int)tasks.size(); ++i) bycount[(int)tasks[i].items.size()].push_back(i);
-    for (auto &kv : bycount)
-      for (size_t q = 0; q < kv.second.size(); q += TASK_LANES) {
-        Slot sl;
-        sl.kind = 1;
-        sl.n = kv.first;
-        for (size_t r = q; r < std::min(kv.second.size(), q + TASK_LANES); ++r) sl.who.push_back(kv.second[r]);
-        sl.rows = 1 + kv.first;
-        ts.items += (int64_t)sl.who.size() * kv.first;
-        ts.pad_items += (int64_t)(TASK_LANES - sl.who.size()) * kv.first;
-        slots.push_back(sl);
+    // tasks by item count, longest first; 32 consecutive ones form a slot
+    // whose length is its longest task's (shorter tasks end in
+    // zero-coefficient items)
+    std::vector<int> bylen(tasks.size());
+    std::iota(bylen.begin(), bylen.end(), 0);
+    std::stable_sort(bylen.begin(), bylen.end(),
+                     [&](int x, int y) { return tasks[x].items.size() > tasks[y].items.size(); });
+    for (size_t q = 0; q < bylen.size(); q += TASK_LANES) {
+      Slot sl;
+      sl.kind = 1;
+      sl.n = (int)tasks[bylen[q]].items.size();
+      for (size_t r = q; r < std::min(bylen.size(), q + TASK_LANES); ++r) {
+        sl.who.push_back(bylen[r]);
+        ts.items += (int64_t)tasks[bylen[r]].items.size();
       }
+      sl.rows = 1 + sl.n;
+      ts.pad_items += (int64_t)TASK_LANES * sl.n;
+      slots.push_back(sl);
+    }
+    ts.pad_items -= ts.items;
     std::map<int, std::vector<int>> byord;
     for (int i = 0; i < (int)shorts.size(); ++i) byord[shorts[i].P].push_back(i);
     for (auto &kv : byord)
@@ -569,7 +577,7 @@ inline TaskSchedule build_tasks(const Schedule &s, int nwarps) {
           if (lane >= (int)sl.who.size()) continue;  // padding: index 0, no coefficients
           const Task &t = tasks[sl.who[lane]];
           for (int d = 0; d < KT; ++d) h[d] = (uint16_t)t.t[d];
-          for (int j = 0; j < sl.n; ++j) {
+          for (int j = 0; j < (int)t.items.size(); ++j) {
             const It &x = t.items[j];
             uint16_t *r = recp(row + 1 + j, lane);
             r[0] = (uint16_t)x.mid;
