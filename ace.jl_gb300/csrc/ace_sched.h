@@ -408,7 +408,7 @@ inline ItemSchedule build_items(const Schedule &s, int nthreads) {
 // items, and the last slot is padded with zero-coefficient tasks; functions
 // of order < K - 1 are "short" items, 32 of equal order per row, evaluated
 // flat (product and local adjoints).  Slots are assigned to the warps of the
-// CTA longest first, each to the warp with the fewest rows.
+// CTA costliest first, each to the warp with the least work.
 //
 // Each warp runs its rows [wrow[w], wrow[w+1]); row r of lane l is record
 // r * 32 + l (16 bytes, 8 uint16): a task header (type 1: t in [0..KT), the
@@ -537,19 +537,23 @@ inline TaskSchedule build_tasks(const Schedule &s, int nwarps) {
         slots.push_back(sl);
       }
   }
-  // balance: longest slots first, each to the warp with the fewest rows
+  // balance: costliest slots first, each to the warp with the least work;
+  // a task header (the task product and the distribution of its adjoint)
+  // costs about three item rows
+  auto cost = [&](const Slot &sl) { return sl.kind == 1 ? sl.rows + 2 : sl.rows; };
   std::vector<size_t> order(slots.size());
   std::iota(order.begin(), order.end(), 0);
-  std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) { return slots[x].rows > slots[y].rows; });
+  std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) { return cost(slots[x]) > cost(slots[y]); });
   std::vector<std::vector<size_t>> own(nwarps);
-  std::vector<int64_t> load(nwarps, 0);
+  std::vector<int64_t> load(nwarps, 0), nrows(nwarps, 0);
   for (size_t si : order) {
     int w = (int)(std::min_element(load.begin(), load.end()) - load.begin());
     own[w].push_back(si);
-    load[w] += slots[si].rows;
+    load[w] += cost(slots[si]);
+    nrows[w] += slots[si].rows;
   }
   ts.wrow.assign(nwarps + 1, 0);
-  for (int w = 0; w < nwarps; ++w) ts.wrow[w + 1] = ts.wrow[w] + (int32_t)load[w];
+  for (int w = 0; w < nwarps; ++w) ts.wrow[w + 1] = ts.wrow[w] + (int32_t)nrows[w];
   ts.rows = ts.wrow[nwarps];
   ts.rec.assign((size_t)ts.rows * TASK_LANES * 8, 0);
   ts.ck.assign((size_t)ts.rows * (1 + G) * TASK_LANES, -1);

@@ -214,9 +214,12 @@ def test_learned_basis_and_derivative(lib, oracle_mod, student, monkeypatch):
     assert relerr(dB, dBref) <= 1e-4
 
 
-def test_force_loss_gradient(lib, student):
+def test_force_loss_gradient(lib, student, monkeypatch):
     torch = _torch()
     spec, mlp = student
+    # the loss below is evaluated with the FP32 MLP that training uses (the
+    # inference calls would otherwise take the BF16 tensor-core radials)
+    monkeypatch.setenv("ACE_B200_MLP", "fp32")
     ctx = learned_context(spec, mlp, precision="fp64")
     ctx.set_params(random_coefficients(spec, seed=5))
     b = random_batch(8, 8, 20, nspecies=NS, seed=21)
