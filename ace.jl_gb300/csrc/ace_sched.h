@@ -507,11 +507,20 @@ inline TaskSchedule build_tasks(const Schedule &s, int nwarps) {
   {
     // tasks by item count, longest first; 32 consecutive ones form a slot
     // whose length is its longest task's (shorter tasks end in
-    // zero-coefficient items)
+    // zero-coefficient items).  Tasks of equal length are taken in a
+    // scrambled order: lexicographic neighbours share most of their A
+    // indices, and 32 of them in one warp would serialise the adjoint's
+    // shared-memory atomics on the same addresses.
+    auto scramble = [](uint32_t x) {
+      x ^= x >> 16; x *= 0x7feb352du; x ^= x >> 15; x *= 0x846ca68bu; x ^= x >> 16;
+      return x;
+    };
     std::vector<int> bylen(tasks.size());
     std::iota(bylen.begin(), bylen.end(), 0);
-    std::stable_sort(bylen.begin(), bylen.end(),
-                     [&](int x, int y) { return tasks[x].items.size() > tasks[y].items.size(); });
+    std::stable_sort(bylen.begin(), bylen.end(), [&](int x, int y) {
+      const size_t nx = tasks[x].items.size(), ny = tasks[y].items.size();
+      return nx > ny || (nx == ny && scramble((uint32_t)x) < scramble((uint32_t)y));
+    });
     for (size_t q = 0; q < bylen.size(); q += TASK_LANES) {
       Slot sl;
       sl.kind = 1;
@@ -527,6 +536,9 @@ inline TaskSchedule build_tasks(const Schedule &s, int nwarps) {
     ts.pad_items -= ts.items;
     std::map<int, std::vector<int>> byord;
     for (int i = 0; i < (int)shorts.size(); ++i) byord[shorts[i].P].push_back(i);
+    for (auto &kv : byord)
+      std::stable_sort(kv.second.begin(), kv.second.end(),
+                       [&](int x, int y) { return scramble((uint32_t)x) < scramble((uint32_t)y); });
     for (auto &kv : byord)
       for (size_t q = 0; q < kv.second.size(); q += TASK_LANES) {
         Slot sl;

@@ -65,7 +65,8 @@ WORKLOADS = {
                            bimodal=(0.6, (40, 80), (8, 20)), fp64_envs=20_000, autotune_envs=20_000),
     "ord4_deg14_4sp": dict(name="ace-invariant 4 species ord4 deg14 L14, 250k envs, J 60% U{40..80} / 40% U{8..20}",
                            maxorder=4, maxdeg=14, maxL=14, nspecies=4, nenv=250_000, jlo=8, jhi=80, seed=2024,
-                           bimodal=(0.6, (40, 80), (8, 20)), fp64_envs=2_000, autotune_envs=5_000),
+                           bimodal=(0.6, (40, 80), (8, 20)), fp64_envs=2_000, autotune_envs=5_000,
+                           autotune_envs_fp64=500),
 }
 DEFAULT_WORKLOAD = "ord5_deg16"
 WORKLOAD = WORKLOADS[DEFAULT_WORKLOAD]
@@ -552,11 +553,14 @@ def main():
             tot = float(t.item())
         return tot, ctx.launch_count() - l0
 
-    # plain FP64 path (the comparison form)
+    # plain FP64 path (the comparison form), autotuned like the others on a
+    # prefix of its own timed batch
     ctx64 = Context(spec, "fp64", device=local)
     ctx64.set_params(c)
     k64 = max(1, min(args.steps, 3))
     n64 = min(nenv, WORKLOAD["fp64_envs"] or nenv)
+    na64 = min(n64, WORKLOAD.get("autotune_envs_fp64", 2000))
+    tuned64 = ctx64.autotune(off_d[:na64 + 1], rr_d, sp_d, E_d[:na64], G_d, reps=1, stream=stream.cuda_stream)
     t64, _ = timed(ctx64, k64, min(args.warmup, 1), n64)
     m64 = int(b.offsets[n64])
     E64 = E_d[:n64].cpu().numpy().copy(); G64 = G_d[:m64].cpu().numpy().copy()
@@ -724,7 +728,9 @@ def main():
             "form": FORMS[chosen][1],
             "autotuned": {"region_kb": tuned % 1000, "schedule": ("trie", "items", "tasks")[tuned // 1000]},
             "chosen_over_fp64": value / v64,
-            "forms": {"fp64": {"value": v64, "ms_per_step": 1e3 * t64 / k64, "envs": n64},
+            "forms": {"fp64": {"value": v64, "ms_per_step": 1e3 * t64 / k64, "envs": n64,
+                               "autotuned": {"region_kb": tuned64 % 1000,
+                                             "schedule": ("trie", "items", "tasks")[tuned64 // 1000]}},
                       "fp32": {"value": nq * k32 * world / t32p, "ms_per_step": 1e3 * t32p / k32, "envs": nq,
                                "error": err32},
                       **cand_forms, **E_only, **basis},
