@@ -418,10 +418,23 @@ __global__ void __launch_bounds__(NT, COMP ? comp_min_blocks<K>() : ef_min_block
       const int lane = tid & 31, wp = tid >> 5;
       const cpx<TG> gone = {TG(1), TG(0)};
       const TL ze = Arith<TL>::zero();
-      for (int64_t row = a.twrow[wp]; row < a.twrow[wp + 1];) {
-        const uint4 hr = __ldg(a.trec + row * 32 + lane);
+      // the next row's record (header, item) is loaded one step ahead, so
+      // its L2 latency overlaps the current step's arithmetic
+      const int64_t rend = a.twrow[wp + 1];
+      auto load_item = [&](int64_t ir, uint4 &rc, TL &c0, TL (&cg)[ITEM_G]) __attribute__((always_inline)) {
+        rc = __ldg(a.trec + ir * 32 + lane);
+        const int64_t cb = ir * (G1 * 32) + lane;
+        c0 = load_coef<TL>(a.tc, cb);
+#pragma unroll
+        for (int g = 0; g < ITEM_G; ++g) cg[g] = load_coef<TL>(a.tc, cb + (g + 1) * 32);
+      };
+      int64_t row = a.twrow[wp];
+      uint4 hr = row < rend ? __ldg(a.trec + row * 32 + lane) : make_uint4(0u, 0u, 0u, 0u);
+      while (row < rend) {
         const int type = (int)(hr.w >> 16), n = (int)(hr.w & 0xffffu);
         const uint32_t hw[2] = {hr.x, hr.y};
+        const int64_t next = row + 1 + (type == 1 ? n : 0);
+        const uint4 hnext = next < rend ? __ldg(a.trec + next * 32 + lane) : make_uint4(0u, 0u, 0u, 0u);
         if (type == 1) {
           int t[KT];
           cpx<TG> ag[KT];
@@ -442,20 +455,23 @@ __global__ void __launch_bounds__(NT, COMP ? comp_min_blocks<K>() : ef_min_block
           }
           cpx<TG> Wt = {TG(0), TG(0)};
           float eterm = 0.0f;  // compensated form: the task's energy terms
-#pragma unroll 2
+          uint4 rcn = make_uint4(0u, 0u, 0u, 0u);
+          TL c0n = ze, cgn[ITEM_G];
+#pragma unroll
+          for (int g = 0; g < ITEM_G; ++g) cgn[g] = ze;
+          if (n > 0) load_item(row + 1, rcn, c0n, cgn);
           for (int j = 0; j < n; ++j) {
-            const int64_t ir = row + 1 + j;
-            const uint4 rc = __ldg(a.trec + ir * 32 + lane);
-            const int mid = (int)(rc.x & 0xffffu), nl = (int)(rc.w & 0xffffu);
-            const int lf[2] = {(int)(rc.x >> 16), (int)(rc.y & 0xffffu)};
-            const int64_t cb = ir * (G1 * 32) + lane;
-            cpx<TL> H = {load_coef<TL>(a.tc, cb), ze};
+            const uint4 rc = rcn;
             TL cg[ITEM_G];
 #pragma unroll
-            for (int g = 0; g < ITEM_G; ++g) {
-              cg[g] = load_coef<TL>(a.tc, cb + (g + 1) * 32);
+            for (int g = 0; g < ITEM_G; ++g) cg[g] = cgn[g];
+            cpx<TL> H = {c0n, ze};
+            if (j + 1 < n) load_item(row + 2 + j, rcn, c0n, cgn);
+            const int mid = (int)(rc.x & 0xffffu), nl = (int)(rc.w & 0xffffu);
+            const int lf[2] = {(int)(rc.x >> 16), (int)(rc.y & 0xffffu)};
+#pragma unroll
+            for (int g = 0; g < ITEM_G; ++g)
               if (g < nl) H = cfma(H, AL[lf[g < 2 ? g : 0]], cg[g]);
-            }
             const cpx<TL> am = AL[mid];
             const cpx<TL> QL = cmul(QtL, am);
             if constexpr (COMP) eterm += re_mul<TL>(QL, H);
@@ -486,7 +502,6 @@ __global__ void __launch_bounds__(NT, COMP ? comp_min_blocks<K>() : ef_min_block
               pre = (d == 0) ? ag[0] : cmul(pre, ag[d]);
             }
           }
-          row += 1 + n;
         } else {
           // short item: P = n < K - 1 indices in [0..P)
           const int P = n;
@@ -521,8 +536,9 @@ __global__ void __launch_bounds__(NT, COMP ? comp_min_blocks<K>() : ef_min_block
               }
             }
           }
-          row += 1;
         }
+        row = next;
+        hr = hnext;
       }
     } else {
       // EF_ITEM_ILP items per thread and iteration, interleaved: their

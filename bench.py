@@ -300,7 +300,10 @@ LEARNED = {
                          name="learned radial K=8 distilled from the ord5 deg16 L16 model, 500k held-out envs, J=30",
                          K=8, Q=8, train_envs=50_000, neighbour_samples=2_000_000, eval_envs=500_000,
                          pretrain_steps=1500, distill_steps=2000, force_envs=2000, force_weight=0.05,
-                         force_loss_weight=0.5, force_batch=32, fp64_check_envs=20_000, seed=2024),
+                         force_loss_weight=0.5, force_batch=32, fp64_check_envs=20_000, seed=2024,
+                         # one species: the network starts from the student's own polynomial
+                         # radials (the truncated teacher basis), not the compressed channels
+                         plain_pretrain=True),
 }
 
 
@@ -358,8 +361,9 @@ def run_learned(args, torch, dist, rank, world, local):
     t0 = time.perf_counter()
     psteps = X["pretrain_steps"] if args.pretrain_steps is None else args.pretrain_steps
     dsteps = X["distill_steps"] if args.distill_steps is None else args.distill_steps
+    plain_pre = args.plain_pretrain or X.get("plain_pretrain", False)
     LR.pretrain_radial(ctx, mlp, spec, nsamples=X["neighbour_samples"], steps=psteps,
-                       teacher=None if args.plain_pretrain else teacher_spec)
+                       teacher=None if plain_pre else teacher_spec)
     nfit = min(20000, train.nenv)
     c0 = LR.fit_coefficients(ctx, spec, LR.sub_batch(train, 0, nfit), Etr[:nfit], forces=forces)
     ctx.set_params(c0)
@@ -456,6 +460,8 @@ def run_learned(args, torch, dist, rank, world, local):
             "reference": "teacher double-float form on every held-out environment; against its FP64 form on the "
                          "first environments: " + json.dumps(ref_check),
             "training": {"neighbour_samples": X["neighbour_samples"], "pretrain_steps": psteps,
+                         "pretrain_targets": "student polynomial radials" if plain_pre else
+                                             "teacher radial x species channels, K leading principal directions per l",
                          "train_envs": X["train_envs"], "distill_steps": dsteps,
                          "force_rows": {"envs": nf if fw > 0 else 0, "weight": fw},
                          "force_loss": {"envs": nf if flw > 0 else 0, "weight": flw, "batch": X["force_batch"]},
