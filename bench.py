@@ -413,6 +413,19 @@ def run_learned(args, torch, dist, rank, world, local):
             tot += s0.elapsed_time(s1) / 1e3
     launches = ctx.launch_count() - l0
     value = nenv * args.steps / tot
+    # the radial MLP's share of a step: the tensor-core inference kernel
+    # alone on the same neighbours (the rest of the step is the energy/force
+    # kernel reading its radials back)
+    Rbuf = torch.empty((ev.nnbr, 2 * mlp.C), dtype=torch.float32, device=dev)
+    ctx.radial_mlp_infer(rr_d, sp_d, Rbuf)
+    torch.cuda.synchronize()
+    s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s0.record(stream)
+    ctx.radial_mlp_infer(rr_d, sp_d, Rbuf, stream=stream.cuda_stream)
+    s1.record(stream)
+    s1.synchronize()
+    mlp_ms = s0.elapsed_time(s1)
+    del Rbuf
 
     def time_form(cx, n, reps=2):
         o = off_d[:n + 1]
@@ -471,6 +484,10 @@ def run_learned(args, torch, dist, rank, world, local):
                       "teacher_fp64": {"value": v64, "envs": n64},
                       "teacher_fp32x2": {"value": vx2, "envs": nenv}},
             "learned_over_teacher_fp64": value / v64,
+            "radial_mlp": {"infer_ms": mlp_ms, "step_ms": 1e3 * tot / args.steps,
+                           "radial_buffer_bytes": int(ev.nnbr) * 2 * mlp.C * 4,
+                           "note": "the inference kernel writes R and dR/dr per neighbour and the energy/force "
+                                   "kernel reads them: radial_buffer_bytes each way per step"},
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peaks["fp32_tflops"], "unit": "TFLOP/s",
                          "frac": achieved / peaks["fp32_tflops"], "traffic": None,
                          "kernel": "mlp_fwd_tc_kernel + ef_kernel<float> (learned radial form); MLP flops counted "
@@ -489,6 +506,8 @@ def main():
     ap.add_argument("--nenv", type=int, default=None, help="smaller workload (profiling only)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--only", default=None, choices=["fp64", "fp32", "fp32x2", "fp32c"],
+                    help="time one form's energy/force launches only (profiling)")
     ap.add_argument("--student-deg", type=int, default=None, help="learned form: student spec degree")
     ap.add_argument("--force-weight", type=float, default=None, help="learned form: weight of gradient rows")
     ap.add_argument("--pretrain-steps", type=int, default=None, help="learned form: radial pretraining steps")
@@ -532,6 +551,32 @@ def main():
     G_d = torch.empty_like(rr_d)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # 256 MB > L2
     stream = torch.cuda.current_stream(dev)
+
+    if args.only:
+        # one form's energy/force launches and nothing else (for profiling:
+        # `warmup` untimed then `steps` timed launches, no autotuning; the
+        # schedule follows ACE_B200_KERNEL)
+        cx = Context(spec, args.only, device=local)
+        cx.set_params(c)
+        for _ in range(args.warmup):
+            cx.energy_forces_device(off_d, rr_d, sp_d, E_d, G_d, stream=stream.cuda_stream, sync=False)
+        torch.cuda.synchronize()
+        tot = 0.0
+        for _ in range(args.steps):
+            flush.zero_()
+            s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s0.record(stream)
+            cx.energy_forces_device(off_d, rr_d, sp_d, E_d, G_d, stream=stream.cuda_stream, sync=False)
+            s1.record(stream)
+            s1.synchronize()
+            tot += s0.elapsed_time(s1) / 1e3
+        cx.sync()
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": nenv * args.steps * world / tot, "unit": UNIT,
+                              "form": args.only, "schedule": os.environ.get("ACE_B200_KERNEL", "default"),
+                              "config": workload_config(b, world), "steps": args.steps, "warmup": args.warmup}),
+                  flush=True)
+        return
 
     def timed(ctx, steps, warmup, n=nenv):
         o_d, e_d = off_d[:n + 1], E_d[:n]
