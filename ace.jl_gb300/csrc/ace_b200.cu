@@ -895,22 +895,24 @@ extern "C" int ace_autotune(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, 
   ACE_CUDA(cudaSetDevice(ctx->device));
   cudaStream_t st = (cudaStream_t)stream;
   const int regions[] = {16, 24, 32, 40, 48, 64};
-  // candidates: the task schedule (orders >= 3), the item runs and, except
-  // for the compensated form (item family only), the trie walk
-  const int variants[] = {2, 1, 0};
-  const int nvariants = ctx->comp ? 2 : 3;
+  // candidates: the task schedule (orders >= 3) at its default and its high
+  // occupancy, the item runs and, except for the compensated form (item
+  // family only), the trie walk
+  const int variants[] = {3, 2, 1, 0};
+  const int nvariants = ctx->comp ? 3 : 4;
   float best = 1e30f;
   int best_region = ctx->region_kb;
-  int best_variant = ctx->use_tasks ? 2 : ctx->use_items ? 1 : 0;
+  int best_variant = ctx->use_tasks ? (ctx->task_high ? 3 : 2) : ctx->use_items ? 1 : 0;
   cudaEvent_t e0, e1;
   ACE_CUDA(cudaEventCreate(&e0));
   ACE_CUDA(cudaEventCreate(&e1));
   reps = std::max(1, std::min(reps, 20));
   for (int vi = 0; vi < nvariants; ++vi) {
     const int variant = variants[vi];
-    if (variant == 2 && !ctx->has_tasks) continue;
+    if (variant >= 2 && !ctx->has_tasks) continue;
     for (int reg : regions) {
-      ctx->use_tasks = variant == 2;
+      ctx->use_tasks = variant >= 2;
+      ctx->task_high = variant == 3;
       ctx->use_items = variant >= 1;
       ctx->region_kb = reg;
       if (kernels_prepare(ctx) != ACE_OK) continue;
@@ -929,7 +931,8 @@ extern "C" int ace_autotune(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, 
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  ctx->use_tasks = best_variant == 2;
+  ctx->use_tasks = best_variant >= 2;
+  ctx->task_high = best_variant == 3;
   ctx->use_items = best_variant >= 1;
   ctx->region_kb = best_region;
   int rc = kernels_prepare(ctx);

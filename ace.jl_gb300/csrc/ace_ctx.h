@@ -53,6 +53,7 @@ struct ace_ctx {
   // task schedule (ace_sched.h build_tasks; orders >= 3): the default
   // correlation walk of single-property energy/force calls
   bool has_tasks = false, use_tasks = false;
+  bool task_high = false;      // the high-occupancy instantiation of the task kernels
   int64_t trows = 0;
   int32_t twrow[5] = {0, 0, 0, 0, 0};
   uint4 *d_trec = nullptr;

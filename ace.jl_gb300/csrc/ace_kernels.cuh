@@ -275,9 +275,13 @@ template <typename TE, int K> constexpr int ef_min_blocks() {
 template <int K> constexpr int comp_min_blocks() { return EF_MIN_BLOCKS > 0 ? EF_MIN_BLOCKS : K <= 4 ? 6 : K == 5 ? 5 : 4; }
 // TASKS (item family, orders >= 3, NT = 128): the correlation phase walks the
 // task schedule (ace_sched.h build_tasks) instead of the per-thread item runs.
+// MINB > 0 overrides the resident CTAs per SM requested from the register
+// allocator (the task-schedule kernels keep little state per thread and have
+// a second, high-occupancy instantiation the autotuner can pick).
 template <typename TE, typename TG, int K, int NT, bool GRAD, bool ITEMS, bool CPX = false, bool COMP = false,
-          bool TASKS = false>
-__global__ void __launch_bounds__(NT, COMP ? comp_min_blocks<K>() : ef_min_blocks<TE, CPX ? K + 1 : K>())
+          bool TASKS = false, int MINB = 0>
+__global__ void __launch_bounds__(NT, MINB > 0 ? MINB
+                                      : COMP ? comp_min_blocks<K>() : ef_min_blocks<TE, CPX ? K + 1 : K>())
     ef_kernel(EFArgs a) {
   static_assert(ITEMS || !CPX, "complex coefficients need the item schedule");
   static_assert(!TASKS || (ITEMS && !CPX && K >= 3 && NT == 128), "the task schedule: real coefficients, K >= 3");

@@ -777,11 +777,11 @@ def main():
             "vs_baseline": None, "dtype": FORMS[chosen][0], "data": "synthetic (seeded)",
             "config": workload_config(b, world),
             "form": FORMS[chosen][1],
-            "autotuned": {"region_kb": tuned % 1000, "schedule": ("trie", "items", "tasks")[tuned // 1000]},
+            "autotuned": {"region_kb": tuned % 1000, "schedule": ("trie", "items", "tasks", "tasks-occ")[tuned // 1000]},
             "chosen_over_fp64": value / v64,
             "forms": {"fp64": {"value": v64, "ms_per_step": 1e3 * t64 / k64, "envs": n64,
                                "autotuned": {"region_kb": tuned64 % 1000,
-                                             "schedule": ("trie", "items", "tasks")[tuned64 // 1000]}},
+                                             "schedule": ("trie", "items", "tasks", "tasks-occ")[tuned64 // 1000]}},
                       "fp32": {"value": nq * k32 * world / t32p, "ms_per_step": 1e3 * t32p / k32, "envs": nq,
                                "error": err32},
                       **cand_forms, **E_only, **basis},

@@ -185,7 +185,8 @@ int ace_basis_noalloc(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, const 
    item runs, or trie walk; the compensated form has no trie walk) and
    shared-memory region size -- and keeps the fastest for this context.
    *choice (optional) receives region_kb + 1000 * algorithm (0 trie walk,
-   1 item runs, 2 task schedule).
+   1 item runs, 2 task schedule, 3 task schedule with the high-occupancy
+   register bound).
    No counterpart in the reference (a GPU launch-configuration choice). */
 int ace_autotune(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, const double *rr,
                  const int32_t *species, double *E, double *dEdrr, int32_t reps, void *stream,

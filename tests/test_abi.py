@@ -82,10 +82,10 @@ def test_energy_force_kernels_do_not_spill(tmp_path):
     dem = subprocess.run(["c++filt"], input="\n".join(names), capture_output=True, text=True).stdout.splitlines()
     checked = 0
     for mangled, d in zip(names, dem):
-        m = re.search(r"ef_kernel<(.+), (\d), 128, true, true, false, (false|true), (false|true)>", d)
+        m = re.search(r"ef_kernel<(.+), (\d), 128, true, true, false, (false|true), (false|true), (\d+)>", d)
         if m and 2 <= int(m.group(2)) <= 5:
             assert report[mangled] == 0, d
             checked += 1
     # {float, double-float, double, compensated} x (item runs: orders 2..5,
-    # task schedule: orders 3..5)
-    assert checked == 28
+    # task schedule: orders 3..5 at the default and the high-occupancy bound)
+    assert checked == 40
