@@ -91,3 +91,22 @@ def test_basis_noalloc_rejects_learned_form(L):
     assert rc == 5  # ACE_ERR_UNSUPPORTED
     assert b"learned" in ctx.lib.ace_last_error_string(ctx.h)
     ctx.close()
+
+
+def test_basis_noalloc_rejects_large_specs(L):
+    """A spec whose per-environment AA vector exceeds the 16 MiB static
+    scratch (4 species, order 4, degree 11: 3.7M AA functions, 29.6 MB in
+    FP64) is rejected with ACE_ERR_UNSUPPORTED before any launch."""
+    torch = pytest.importorskip("torch")
+    spec = symmetric_basis(4, 11, maxL=11, nspecies=4)
+    assert spec.nAA * 8 > 16 << 20
+    ctx = L.Context(spec, "fp64")
+    b = random_batch(4, 8, 12, nspecies=4, seed=1)
+    off = torch.from_numpy(b.offsets).cuda()
+    rr = torch.from_numpy(b.rr).cuda()
+    sp = torch.from_numpy(b.species).cuda()
+    B = torch.empty((b.nenv, spec.nB), dtype=torch.float64, device="cuda")
+    rc = ctx.lib.ace_basis_noalloc(ctx.h, b.nenv, L._ptr(off), L._ptr(rr), L._ptr(sp), L._ptr(B), None)
+    assert rc == 5  # ACE_ERR_UNSUPPORTED
+    assert b"16 MiB" in ctx.lib.ace_last_error_string(ctx.h)
+    ctx.close()
