@@ -27,7 +27,7 @@ EXPORTED = ("ace_ctx_create", "ace_ctx_destroy", "ace_set_params", "ace_set_ctil
             "ace_set_params_multi", "ace_energy_forces_multi", "ace_autotune", "ace_set_radial_mlp",
             "ace_radial_mlp_params", "ace_radial_mlp_forward", "ace_radial_mlp_backward",
             "ace_energy_radial_adjoint", "ace_adam_step", "ace_radial_mlp_get_params", "ace_radial_mlp_infer",
-            "ace_set_ctilde_complex")
+            "ace_set_ctilde_complex", "ace_set_energy_tolerance", "ace_energy_error_estimates")
 
 
 class AceError(RuntimeError):
@@ -95,13 +95,16 @@ def load(path: str | None = None):
     lib.ace_last_error_string.restype = C.c_char_p
     lib.ace_launch_count.argtypes = [P]
     lib.ace_launch_count.restype = C.c_int64
+    lib.ace_set_energy_tolerance.argtypes = [P, C.c_double]
+    lib.ace_energy_error_estimates.argtypes = [P, C.c_int64, P, P]
     for name in ("ace_ctx_create", "ace_ctx_destroy", "ace_set_params", "ace_set_ctilde",
                  "ace_energy_forces", "ace_energy", "ace_basis", "ace_sync", "ace_get_spec_sizes",
                  "ace_basis_noalloc", "ace_adjoint_eval_d",
             "ace_set_params_multi", "ace_energy_forces_multi", "ace_autotune", "ace_set_radial_mlp",
                  "ace_radial_mlp_params", "ace_radial_mlp_forward", "ace_radial_mlp_backward",
                  "ace_energy_radial_adjoint", "ace_adam_step", "ace_radial_mlp_get_params",
-                 "ace_radial_mlp_infer", "ace_set_ctilde_complex"):
+                 "ace_radial_mlp_infer", "ace_set_ctilde_complex", "ace_set_energy_tolerance",
+                 "ace_energy_error_estimates"):
         getattr(lib, name).restype = C.c_int
     _lib = lib
     return lib
@@ -275,6 +278,21 @@ class Context:
         st = None if stream is None else C.c_void_p(int(stream))
         self._check(self.lib.ace_energy_forces(self.h, E.numel(), _ptr(offsets), _ptr(rr), _ptr(species),
                                                _ptr(E), _ptr(G), flags, st))
+
+    # error control of the compensated form ("fp32c")
+    def set_energy_tolerance(self, tol: float):
+        """Environments whose estimated energy error exceeds tol * max(|E|,
+        rms E of the launch) are evaluated again in double-float (0: off)."""
+        self._check(self.lib.ace_set_energy_tolerance(self.h, float(tol)))
+
+    def energy_error_estimates(self, n: int | None = None):
+        """(estimates of the last energy call's first n environments (None:
+        only the count), environments re-evaluated since creation)."""
+        refined = C.c_int64(0)
+        est = None if n is None else np.zeros(n, dtype=np.float64)
+        self._check(self.lib.ace_energy_error_estimates(self.h, 0 if n is None else n,
+                                                        None if est is None else _ptr(est), C.byref(refined)))
+        return est, int(refined.value)
 
     def autotune(self, offsets, rr, species, E, G, reps=3, stream=None):
         """Pick the fastest launch configuration on this device batch (torch

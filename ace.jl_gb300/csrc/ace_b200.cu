@@ -136,6 +136,7 @@ extern "C" int ace_ctx_create(const ace_spec_bundle *s, int32_t prec, int32_t de
   ctx->device = device;
   ctx->prec = prec;
   ctx->comp = comp;
+  ctx->guard_tol = comp ? 1e-6 : 0.0;
   ctx->nR = s->nR; ctx->nA = s->nA; ctx->nAA = s->nAA; ctx->nB = s->nB;
   ctx->maxord = s->maxord; ctx->nspecies = s->nspecies;
   ctx->pl = s->pl; ctx->pr = s->pr; ctx->tp = s->tp;
@@ -253,16 +254,21 @@ extern "C" int ace_ctx_create(const ace_spec_bundle *s, int32_t prec, int32_t de
           g_create_error = ctx->err;
           return fail(rc);
         }
-        const size_t tsz = comp ? 4 : csz;
-        void **dst = comp ? (void **)&ctx->d_tc32 : &ctx->d_tc;
-        if (cudaMalloc(dst, ctx->tk.size() * tsz) != cudaSuccess) {
-          g_create_error = "cudaMalloc failed";
-          return fail(ACE_ERR_ALLOC);
-        }
-        ctx->allocs.push_back(*dst);
-        if (cudaMemset(*dst, 0, ctx->tk.size() * tsz) != cudaSuccess) {
-          g_create_error = "cudaMemset failed";
-          return fail(ACE_ERR_CUDA);
+        // coefficients in the energy type (a compensated context: also in
+        // FP32 for its own kernels; the double-float ones serve its
+        // re-evaluations)
+        for (int copy = 0; copy < (comp ? 2 : 1); ++copy) {
+          const size_t tsz = copy ? 4 : csz;
+          void **dst = copy ? (void **)&ctx->d_tc32 : &ctx->d_tc;
+          if (cudaMalloc(dst, ctx->tk.size() * tsz) != cudaSuccess) {
+            g_create_error = "cudaMalloc failed";
+            return fail(ACE_ERR_ALLOC);
+          }
+          ctx->allocs.push_back(*dst);
+          if (cudaMemset(*dst, 0, ctx->tk.size() * tsz) != cudaSuccess) {
+            g_create_error = "cudaMemset failed";
+            return fail(ACE_ERR_CUDA);
+          }
         }
       }
       if (const char *kenv2 = getenv("ACE_B200_KERNEL"))
@@ -363,6 +369,8 @@ extern "C" int ace_ctx_destroy(ace_ctx *ctx) {
   for (void *p : ctx->allocs) cudaFree(p);
   if (ctx->d_stage) cudaFree(ctx->d_stage);
   if (ctx->d_scratch) cudaFree(ctx->d_scratch);
+  if (ctx->d_gest) cudaFree(ctx->d_gest);
+  if (ctx->d_glist) cudaFree(ctx->d_glist);
   if (ctx->d_wstage) cudaFree(ctx->d_wstage);
   if (ctx->d_ic_multi) cudaFree(ctx->d_ic_multi);
   for (cudaStream_t st : {ctx->s_in, ctx->s_comp, ctx->s_out})
@@ -415,10 +423,9 @@ static int push_ctilde(ace_ctx *ctx) {
       std::vector<float> c(ctx->tk.size());
       for (size_t j = 0; j < c.size(); ++j) c[j] = (float)tval((int64_t)j);
       ACE_CUDA(cudaMemcpy(ctx->d_tc32, c.data(), c.size() * sizeof(float), cudaMemcpyHostToDevice));
-    } else {
-      rc = pack_coefs(ctx, ctx->d_tc, (int64_t)ctx->tk.size(), tval);
-      if (rc) return rc;
     }
+    rc = pack_coefs(ctx, ctx->d_tc, (int64_t)ctx->tk.size(), tval);
+    if (rc) return rc;
   }
   const int64_t n = (int64_t)ctx->sslot.size();
   auto val = [&](int64_t j) { return ctx->sslot[j] < 0 ? 0.0 : ctx->sw[j] * ctx->ctilde[ctx->sslot[j]]; };
@@ -721,6 +728,8 @@ static int energy_forces_pipelined(ace_ctx *ctx, int64_t nEnv, const int64_t *of
   const size_t o_E = need; need += al256(nEnv * sizeof(double));
   const size_t o_G = need; if (G) need += al256(std::max<int64_t>(nNbr, 1) * 3 * sizeof(double));
   if ((rc = ensure_stage(ctx, need))) return rc;
+  // the compensated form's error estimates of every chunk (at offset e0)
+  if (ctx->comp && (rc = guard_prepare(ctx, nEnv))) return rc;
   char *base = (char *)ctx->d_stage;
   int64_t *d_off = (int64_t *)(base + o_off);
   double *d_rr = (double *)(base + o_rr);
@@ -751,7 +760,10 @@ static int energy_forces_pipelined(ace_ctx *ctx, int64_t nEnv, const int64_t *of
     if (!ck(cudaEventRecord(ev_in, ctx->s_in), "event record") ||
         !ck(cudaStreamWaitEvent(ctx->s_comp, ev_in, 0), "stream wait"))
       break;
-    if ((err = launch_energy_forces(ctx, e1 - e0, d_off + e0, d_rr, d_sp, d_E + e0, d_G, ctx->s_comp))) break;
+    ctx->guard_off = e0;
+    err = launch_energy_forces(ctx, e1 - e0, d_off + e0, d_rr, d_sp, d_E + e0, d_G, ctx->s_comp);
+    ctx->guard_off = 0;
+    if (err) break;
     if (!ck(cudaEventRecord(ev_comp, ctx->s_comp), "event record") ||
         !ck(cudaStreamWaitEvent(ctx->s_out, ev_comp, 0), "stream wait"))
       break;

@@ -65,6 +65,19 @@ struct ace_ctx {
   // other path; the single-property item kernel reads FP32 coefficients d_ic32
   bool comp = false;
   float *d_ic32 = nullptr;     // [(G+1) * item_n] coefficients in FP32
+  // its error control (ace_set_energy_tolerance, ace_guard.cu): the kernels
+  // write each environment's rounding scale to d_gest (offset guard_off
+  // within the call, for the chunks of the host-buffer pipeline); the
+  // environments over the tolerance are listed in d_glist and evaluated
+  // again by the double-float kernel; d_gsum holds a launch's sum of E^2
+  // and list length, d_gtotal the re-evaluations since creation
+  double guard_tol = 0.0;
+  float *d_gest = nullptr;
+  int64_t *d_glist = nullptr;
+  int64_t guard_cap = 0, guard_off = 0, guard_last = 0;
+  double guard_kappa_last = 0.0;  // the factor of the last call's estimates
+  void *d_gsum = nullptr;
+  unsigned long long *d_gtotal = nullptr;
   int64_t item_n = 0;
   uint4 *d_irec = nullptr;
   void *d_ic = nullptr;        // [(G+1) * item_n] coefficients in the energy type
@@ -146,8 +159,18 @@ int launch_energy_forces(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const d
 void *ef_func_cplx(const ace_ctx *ctx, bool grad);
 // compensated-form energy/force kernels (ace_launch_comp.cu)
 void *ef_func_comp(const ace_ctx *ctx);
-// task-schedule energy/force kernels (ace_launch_tasks.cu)
+// task-schedule energy/force kernels (ace_launch_tasks.cu); _df: the
+// double-float kernel also in a compensated context (its re-evaluations)
 void *ef_func_tasks(const ace_ctx *ctx, bool grad);
+void *ef_func_tasks_df(const ace_ctx *ctx, bool grad);
+// error control of the compensated form (ace_guard.cu): guard_prepare grows
+// the estimate and list arrays to n environments; guard_flag lists the
+// launch's environments whose estimate est[0 .. nEnv) is over the tolerance
+// (their number at guard_count, on the device)
+int guard_prepare(ace_ctx *ctx, int64_t n);
+double guard_kappa(const ace_ctx *ctx);
+int guard_flag(ace_ctx *ctx, int64_t nEnv, const double *E, const float *est, cudaStream_t st);
+const int32_t *guard_count(const ace_ctx *ctx);
 int launch_basis(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const double *rr,
                  const int32_t *sp, double *B, double *dB, cudaStream_t st);
 int launch_dbasis(ace_ctx *ctx, int64_t nEnv, const int64_t *off_d, const int64_t *off_h, const double *rr,

@@ -85,6 +85,14 @@ struct EFArgs {
   const void *tc;
   int32_t twrow[5];
   int *status;
+  // compensated form: est[e] (if set) receives the environment's energy
+  // rounding scale sqrt(sum_g S_g^2) 2^-24, S_g the sum of |products| that
+  // share a rounding (a task of the task schedule, an item of the item runs)
+  float *est;
+  // environment list (if set): the launch evaluates environments
+  // elist[0 .. *ecount) of the batch instead of 0 .. nEnv
+  const int64_t *elist;
+  const int32_t *ecount;
   // aa_kernel output
   void *AAout;
   int64_t ldE;
@@ -149,6 +157,28 @@ template <> __device__ __forceinline__ double load_table<double>(const void *p, 
 template <> __device__ __forceinline__ df load_table<df>(const void *p, int i) {
   const float2 v = ((const float2 *)p)[i];
   return {v.x, v.y};
+}
+
+// two block sums at once (blocks of at most 16 warps); valid in thread 0
+__device__ __forceinline__ void block_sum2(double &v, double &u, double *red) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    v += __shfl_xor_sync(0xffffffffu, v, o);
+    u += __shfl_xor_sync(0xffffffffu, u, o);
+  }
+  if (lane == 0) { red[w] = v; red[16 + w] = u; }
+  __syncthreads();
+  if (w == 0) {
+    v = lane < nw ? red[lane] : 0.0;
+    u = lane < nw ? red[16 + lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      v += __shfl_xor_sync(0xffffffffu, v, o);
+      u += __shfl_xor_sync(0xffffffffu, u, o);
+    }
+  }
+  __syncthreads();
 }
 
 __device__ __forceinline__ double block_sum(double v, double *red) {
@@ -321,8 +351,10 @@ __global__ void __launch_bounds__(NT, MINB > 0 ? MINB
   Tables<TG> tbG;
   tbG.bind(tabG, a.nR, a.L, a.pl, a.pr, a.tp);
   const int64_t ntot = a.off[a.nEnv];
+  const int64_t nrun = a.elist ? (int64_t)*a.ecount : a.nEnv;
 
-  for (int64_t e = blockIdx.x; e < a.nEnv; e += gridDim.x) {
+  for (int64_t q = blockIdx.x; q < nrun; q += gridDim.x) {
+    const int64_t e = a.elist ? a.elist[q] : q;
     const int64_t o0 = a.off[e], o1 = a.off[e + 1];
     if (o0 < 0 || o1 < o0 || o1 > ntot) {
       if (tid == 0) {
@@ -355,6 +387,7 @@ __global__ void __launch_bounds__(NT, MINB > 0 ? MINB
       }
     };
     TE eacc = Arith<TE>::zero();
+    float est2 = 0.0f;  // compensated form: sum of squared rounding groups
     // the correlation phase reads A in its own arithmetic type
     const cpx<TL> *AL;
     if constexpr (COMP) AL = (const cpx<TL> *)AG; else AL = (const cpx<TL> *)AE;
@@ -459,6 +492,7 @@ __global__ void __launch_bounds__(NT, MINB > 0 ? MINB
           }
           cpx<TG> Wt = {TG(0), TG(0)};
           float eterm = 0.0f;  // compensated form: the task's energy terms
+          float esz = 0.0f;    // and the sum of their products' magnitudes
           uint4 rcn = make_uint4(0u, 0u, 0u, 0u);
           TL c0n = ze, cgn[ITEM_G];
 #pragma unroll
@@ -478,8 +512,13 @@ __global__ void __launch_bounds__(NT, MINB > 0 ? MINB
               if (g < nl) H = cfma(H, AL[lf[g < 2 ? g : 0]], cg[g]);
             const cpx<TL> am = AL[mid];
             const cpx<TL> QL = cmul(QtL, am);
-            if constexpr (COMP) eterm += re_mul<TL>(QL, H);
-            else eacc = eacc + re_mul<TE>(QL, H);
+            if constexpr (COMP) {
+              const float p1 = QL.re * H.re, p2 = QL.im * H.im;
+              eterm += p1 - p2;
+              esz += fabsf(p1) + fabsf(p2);
+            } else {
+              eacc = eacc + re_mul<TE>(QL, H);
+            }
             if (GRAD) {
               const cpx<TG> amg = {lower<TG>(am.re), lower<TG>(am.im)};
               cpx<TG> QG;
@@ -493,7 +532,10 @@ __global__ void __launch_bounds__(NT, MINB > 0 ? MINB
               Wt = cadd(Wt, cmul(h, amg));
             }
           }
-          if constexpr (COMP) eacc = eacc + df{eterm, 0.0f};
+          if constexpr (COMP) {
+            eacc = eacc + df{eterm, 0.0f};
+            est2 = fmaf(esz, esz, est2);
+          }
           if (GRAD) {
             // W over the task prefix: prefix and suffix products
             cpx<TG> pre = gone;
@@ -523,8 +565,13 @@ __global__ void __launch_bounds__(NT, MINB > 0 ? MINB
               ag[d] = {lower<TG>(av.re), lower<TG>(av.im)};
             }
           }
-          if constexpr (COMP) eacc = eacc + df{c * p.re, 0.0f};
-          else eacc = eacc + c * p.re;
+          if constexpr (COMP) {
+            const float t = c * p.re;
+            eacc = eacc + df{t, 0.0f};
+            est2 = fmaf(t, t, est2);
+          } else {
+            eacc = eacc + c * p.re;
+          }
           if (GRAD) {
             const TG cG = lower<TG>(c);
             cpx<TG> pre = gone;
@@ -663,12 +710,15 @@ __global__ void __launch_bounds__(NT, MINB > 0 ? MINB
               }
               if constexpr (COMP) {
                 // the item's prefix product is the path product at its depth
-                // (a term per depth, kept by a select: no indexed access)
+                // (selected, not indexed: Q stays in registers)
+                cpx<TG> qd = Q[0];
 #pragma unroll
-                for (int d = 0; d < KP; ++d) {
-                  const float t = re_mul<TG>(Q[d], h);
-                  eterm += (d == cP - 1) ? t : 0.0f;
-                }
+                for (int d = 1; d < KP; ++d)
+                  if (d == cP - 1) qd = Q[d];
+                const float p1 = qd.re * h.re, p2 = qd.im * h.im;
+                eterm += p1 - p2;
+                const float sz = fabsf(p1) + fabsf(p2);
+                est2 = fmaf(sz, sz, est2);
               }
               // only full-length prefixes carry leaves
               const cpx<TG> bG = Q[KP - 1];
@@ -776,8 +826,13 @@ __global__ void __launch_bounds__(NT, MINB > 0 ? MINB
         const cpx<TG> d = D[i];
         eloc += (double)d.re * (double)lo.re - (double)d.im * (double)lo.im;
       }
-      const double esum = block_sum(eloc, red);
-      if (tid == 0) a.E[e] = a.c0 + esum;
+      static_assert(!COMP || NT <= 512, "block_sum2: at most 16 warps");
+      double esum = eloc, esq = (double)est2;
+      block_sum2(esum, esq, red);
+      if (tid == 0) {
+        a.E[e] = a.c0 + esum;
+        if (a.est) a.est[e] = (float)(sqrt(esq) * 0x1p-24);
+      }
       if (!a.G && !a.GR) continue;  // energies only
     }
     // ---------------- phase 3: forces

@@ -127,6 +127,8 @@ int kernels_prepare(ace_ctx *ctx) {
   std::vector<void *> fs = {ef_func(ctx, false), ef_func(ctx, true)};
   if (uses_comp(ctx)) fs.push_back(ef_func_comp(ctx));
   if (ctx->has_tasks) { fs.push_back(ef_func_tasks(ctx, false)); fs.push_back(ef_func_tasks(ctx, true)); }
+  // (a compensated context's re-evaluations: the double-float task kernels)
+  if (ctx->comp && ctx->has_tasks) { fs.push_back(ef_func_tasks_df(ctx, false)); fs.push_back(ef_func_tasks_df(ctx, true)); }
   for (void *f : fs)
     if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, ctx->smem_optin) != cudaSuccess) {
       ctx->err = "cudaFuncSetAttribute failed";
@@ -193,11 +195,41 @@ int launch_energy_forces(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const d
       return ACE_ERR_CUDA;
     }
   }
+  // the compensated form estimates each environment's rounding error
+  // (ace_guard.cu) and, with a tolerance set, evaluates the environments
+  // over it again in double-float
+  const bool guard = !ic && !cpx && uses_comp(ctx);
+  if (guard) {
+    int rc = guard_prepare(ctx, ctx->guard_off + nEnv);
+    if (rc) return rc;
+    a.est = ctx->d_gest + ctx->guard_off;
+    ctx->guard_last = ctx->guard_off + nEnv;
+    ctx->guard_kappa_last = guard_kappa(ctx);
+  }
   const int grid = (int)std::min<int64_t>(nEnv, ctx->grid);
   void *args[] = {&a};
   cudaError_t e = cudaLaunchKernel(f, dim3(grid), dim3(NT), args, smem, st);
   ctx->launches += 1;
   if (e != cudaSuccess) { ctx->err = cudaGetErrorString(e); return ACE_ERR_CUDA; }
+  if (guard && ctx->guard_tol > 0.0) {
+    int rc = guard_flag(ctx, nEnv, E, a.est, st);
+    if (rc) return rc;
+    EFArgs b = make_args(ctx, nEnv, off, rr, sp, E, G);
+    b.elist = ctx->d_glist;
+    b.ecount = guard_count(ctx);
+    void *g;
+    if (ctx->has_tasks) {
+      g = ef_func_tasks_df(ctx, G != nullptr);
+      b.tc = ctx->d_tc;
+    } else {
+      g = ef_func_t<df, float>(ctx, G != nullptr);
+      b.ic = ctx->d_ic;
+    }
+    void *bargs[] = {&b};
+    e = cudaLaunchKernel(g, dim3(grid), dim3(NT), bargs, ctx->smem, st);
+    ctx->launches += 1;
+    if (e != cudaSuccess) { ctx->err = cudaGetErrorString(e); return ACE_ERR_CUDA; }
+  }
   return ACE_OK;
 }
 

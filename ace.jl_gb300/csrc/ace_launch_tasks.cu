@@ -39,6 +39,10 @@ static void *tk_occ(const ace_ctx *ctx) {
   return tk_k<TE, TG, GRAD, COMP, 0>(ctx->maxord);
 }
 
+void *ef_func_tasks_df(const ace_ctx *ctx, bool grad) {
+  return grad ? tk_k<df, float, true, false, 0>(ctx->maxord) : tk_k<df, float, false, false, 0>(ctx->maxord);
+}
+
 void *ef_func_tasks(const ace_ctx *ctx, bool grad) {
   if (ctx->comp) return tk_occ<df, float, true, true>(ctx);
   switch (ctx->prec) {

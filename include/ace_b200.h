@@ -64,8 +64,10 @@ enum {
   ACE_PREC_FP32_COMP = 5    /* compensated: Rn, Ylm and A in double-float; the correlation
                                products, adjoint and forces in FP32 on A rounded to FP32, the
                                energy summed in double-float and corrected to first order for
-                               that rounding (E += Re sum_i dE/dA_i A_lo_i); every other path
-                               as ACE_PREC_FP32X2 */
+                               that rounding (E += Re sum_i dE/dA_i A_lo_i); environments whose
+                               estimated energy error exceeds a tolerance are evaluated again in
+                               double-float (ace_set_energy_tolerance); every other path as
+                               ACE_PREC_FP32X2 */
 };
 
 /* flags for the evaluation calls */
@@ -149,6 +151,28 @@ int ace_energy_forces(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, const 
                       void *stream);
 int ace_energy(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, const double *rr,
                const int32_t *species, double *E, int32_t flags, void *stream);
+
+/* Error control of the compensated form (ACE_PREC_FP32_COMP; other modes
+   return ACE_ERR_UNSUPPORTED).  Its rounding errors are those of the FP32
+   correlation products; products that share a rounding (the prefix of a
+   task, the terms of an item) form a group g with summed magnitude S_g, and
+   every single-property ace_energy_forces / ace_energy launch estimates
+   each environment's energy error as est_e = k sqrt(sum_g S_g^2) 2^-24,
+   k = 5 on the task schedule and 7 on the item runs (measured against FP64
+   on orders 4 and 5: errors up to 3.9 and 5.5 times the root sum square).
+   Environments with est_e > tol * max(|E_e|, rms of E over the launch) are
+   then evaluated again in double-float (ACE_PREC_FP32X2 arithmetic, energy
+   error ~1e-12) within the same call, on the device (no synchronisation:
+   the call stays asynchronous and capturable).  tol = 0 turns the
+   re-evaluation off; the default is 1e-6.  No counterpart in the reference
+   (its evaluation is FP64). */
+int ace_set_energy_tolerance(ace_ctx *ctx, double tol);
+/* est_e of the last single-property energy call's first nEnv environments
+   (est: host array, may be NULL; the estimate of the compensated
+   evaluation also for re-evaluated environments) and the number of
+   environments re-evaluated since the context was created (refined, may be
+   NULL).  Synchronises with the context's work. */
+int ace_energy_error_estimates(ace_ctx *ctx, int64_t nEnv, double *est, int64_t *refined);
 
 /* Symmetric basis B[e*nB + b]; if dB != NULL also
    dB[(j*nB + b)*3 + a] = dB_b(env of j)/d rr_j[a]. */
