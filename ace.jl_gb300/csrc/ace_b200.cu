@@ -353,6 +353,9 @@ extern "C" int ace_ctx_create(const ace_spec_bundle *s, int32_t prec, int32_t de
     return fail(ACE_ERR_ALLOC);
   }
   if (cudaDeviceSynchronize() != cudaSuccess) { g_create_error = "device sync failed"; return fail(ACE_ERR_CUDA); }
+  // a fixed shared region (KB) instead of the default, as ace_autotune would
+  // choose it (for profiling one configuration)
+  if (const char *renv = getenv("ACE_B200_REGION_KB")) ctx->region_kb = std::max(8, std::min(96, atoi(renv)));
   rc = kernels_prepare(ctx);
   if (rc != ACE_OK) { g_create_error = ctx->err; return fail(rc); }
   // the allocation-free basis entry point's scratch address (its outcome is

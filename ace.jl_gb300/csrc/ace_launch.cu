@@ -180,9 +180,21 @@ int launch_energy_forces(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const d
   if (ic) { a.ic = ic; a.c0 = c0; }
   void *f = ef_func(ctx, G != nullptr);
   size_t smem = ctx->smem;
-  if (!ic && !cpx) {
-    // the single-property kernel: task schedule, compensated form (whose
-    // energies need the adjoint, with or without gradients) or item runs
+  // energies only in a compensated context: the double-float energy kernel,
+  // which needs no adjoint (the compensated energy's correction does), is
+  // faster there and exact to ~1e-12
+  const bool comp_eonly = !ic && !cpx && uses_comp(ctx) && G == nullptr;
+  if (comp_eonly) {
+    if (uses_tasks(ctx)) {
+      f = ef_func_tasks_df(ctx, false);
+      a.tc = ctx->d_tc;
+    } else {
+      f = ef_func_t<df, float>(ctx, false);
+      a.ic = ctx->d_ic;
+    }
+    ctx->guard_last = 0;  // (no estimates)
+  } else if (!ic && !cpx) {
+    // the single-property kernel: task schedule, compensated form or item runs
     const void *coef;
     f = ef_main(ctx, G != nullptr, &coef, &smem);
     if (uses_tasks(ctx)) a.tc = coef;
@@ -198,7 +210,7 @@ int launch_energy_forces(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const d
   // the compensated form estimates each environment's rounding error
   // (ace_guard.cu) and, with a tolerance set, evaluates the environments
   // over it again in double-float
-  const bool guard = !ic && !cpx && uses_comp(ctx);
+  const bool guard = !ic && !cpx && uses_comp(ctx) && !comp_eonly;
   if (guard) {
     int rc = guard_prepare(ctx, ctx->guard_off + nEnv);
     if (rc) return rc;

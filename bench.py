@@ -556,7 +556,7 @@ def main():
     if args.only:
         # one form's energy/force launches and nothing else (for profiling:
         # `warmup` untimed then `steps` timed launches, no autotuning; the
-        # schedule follows ACE_B200_KERNEL)
+        # schedule follows ACE_B200_KERNEL, the shared region ACE_B200_REGION_KB)
         cx = Context(spec, args.only, device=local)
         cx.set_params(c)
         for _ in range(args.warmup):
@@ -575,6 +575,7 @@ def main():
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": nenv * args.steps * world / tot, "unit": UNIT,
                               "form": args.only, "schedule": os.environ.get("ACE_B200_KERNEL", "default"),
+                              "region_kb": os.environ.get("ACE_B200_REGION_KB", "default"),
                               "config": workload_config(b, world), "steps": args.steps, "warmup": args.warmup}),
                   flush=True)
         return

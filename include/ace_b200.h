@@ -156,7 +156,7 @@ int ace_energy(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, const double 
    return ACE_ERR_UNSUPPORTED).  Its rounding errors are those of the FP32
    correlation products; products that share a rounding (the prefix of a
    task, the terms of an item) form a group g with summed magnitude S_g, and
-   every single-property ace_energy_forces / ace_energy launch estimates
+   every single-property ace_energy_forces launch with gradients estimates
    each environment's energy error as est_e = k sqrt(sum_g S_g^2) 2^-24,
    k = 5 on the task schedule and 7 on the item runs (measured against FP64
    on orders 4 and 5: errors up to 3.9 and 5.5 times the root sum square).
@@ -164,10 +164,12 @@ int ace_energy(ace_ctx *ctx, int64_t nEnv, const int64_t *offsets, const double 
    then evaluated again in double-float (ACE_PREC_FP32X2 arithmetic, energy
    error ~1e-12) within the same call, on the device (no synchronisation:
    the call stays asynchronous and capturable).  tol = 0 turns the
-   re-evaluation off; the default is 1e-6.  No counterpart in the reference
-   (its evaluation is FP64). */
+   re-evaluation off; the default is 1e-6.  Energy-only calls (ace_energy,
+   or dEdrr = NULL) of a compensated context run the double-float energy
+   kernel (no adjoint needed, energy error ~1e-12) and make no estimates.
+   No counterpart in the reference (its evaluation is FP64). */
 int ace_set_energy_tolerance(ace_ctx *ctx, double tol);
-/* est_e of the last single-property energy call's first nEnv environments
+/* est_e of the last single-property energy/gradient call's first nEnv environments
    (est: host array, may be NULL; the estimate of the compensated
    evaluation also for re-evaluated environments) and the number of
    environments re-evaluated since the context was created (refined, may be
