@@ -109,6 +109,7 @@ struct ace_ctx {
   // launch configuration chosen at create time (and by ace_autotune)
   int region_kb = 40;          // shared region for neighbour slabs / private adjoint bins
   int nt = 128, chunkE = 32, chunkG = 16, npriv = 32, grid = 0;
+  int grid_df[2] = {0, 0};     // compensated context: its double-float kernels' grids (energy, E+F)
   size_t smem = 0, smem_comp = 0;
   int aa_chunk = 32, aa_grid = 0;
   size_t aa_smem = 0;

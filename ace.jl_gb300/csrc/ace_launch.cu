@@ -142,6 +142,17 @@ int kernels_prepare(ace_ctx *ctx) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, f, NT, sm);
   }
   ctx->grid = ctx->nsm * std::max(occ, 1);
+  // a compensated context's double-float launches (energies only, and the
+  // re-evaluations) have their own occupancy: a grid of more CTAs than can
+  // be resident would run its last CTAs' environments in a second wave
+  if (ctx->comp) {
+    for (int g = 0; g < 2; ++g) {
+      void *f = uses_tasks(ctx) ? ef_func_tasks_df(ctx, g == 1) : ef_func_t<df, float>(ctx, g == 1);
+      int o = 1;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, f, NT, ctx->smem);
+      ctx->grid_df[g] = ctx->nsm * std::max(o, 1);
+    }
+  }
   // basis path (AA materialisation)
   ctx->aa_chunk = std::max(1, std::min(256 / (ctx->L + 1), (32 * 1024) / slabE));
   EFLayout la = ef_layout(ctx->ntab, nRs, ctx->L, ctx->nA, ctx->aa_chunk, 1, 0, 256, sE, sE, true);
@@ -218,7 +229,7 @@ int launch_energy_forces(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const d
     ctx->guard_last = ctx->guard_off + nEnv;
     ctx->guard_kappa_last = guard_kappa(ctx);
   }
-  const int grid = (int)std::min<int64_t>(nEnv, ctx->grid);
+  const int grid = (int)std::min<int64_t>(nEnv, comp_eonly ? ctx->grid_df[0] : ctx->grid);
   void *args[] = {&a};
   cudaError_t e = cudaLaunchKernel(f, dim3(grid), dim3(NT), args, smem, st);
   ctx->launches += 1;
@@ -229,8 +240,9 @@ int launch_energy_forces(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const d
     EFArgs b = make_args(ctx, nEnv, off, rr, sp, E, G);
     b.elist = ctx->d_glist;
     b.ecount = guard_count(ctx);
+    // (the schedule the context was tuned to)
     void *g;
-    if (ctx->has_tasks) {
+    if (uses_tasks(ctx)) {
       g = ef_func_tasks_df(ctx, G != nullptr);
       b.tc = ctx->d_tc;
     } else {
@@ -238,7 +250,8 @@ int launch_energy_forces(ace_ctx *ctx, int64_t nEnv, const int64_t *off, const d
       b.ic = ctx->d_ic;
     }
     void *bargs[] = {&b};
-    e = cudaLaunchKernel(g, dim3(grid), dim3(NT), bargs, ctx->smem, st);
+    const int gridb = (int)std::min<int64_t>(nEnv, ctx->grid_df[G != nullptr ? 1 : 0]);
+    e = cudaLaunchKernel(g, dim3(gridb), dim3(NT), bargs, ctx->smem, st);
     ctx->launches += 1;
     if (e != cudaSuccess) { ctx->err = cudaGetErrorString(e); return ACE_ERR_CUDA; }
   }
