@@ -713,8 +713,11 @@ __global__ void __launch_bounds__(NT, MINB > 0 ? MINB
                 // (selected, not indexed: Q stays in registers)
                 cpx<TG> qd = Q[0];
 #pragma unroll
-                for (int d = 1; d < KP; ++d)
-                  if (d == cP - 1) qd = Q[d];
+                for (int d = 1; d < KP; ++d) {
+                  const bool at = d == cP - 1;
+                  qd.re = at ? Q[d].re : qd.re;
+                  qd.im = at ? Q[d].im : qd.im;
+                }
                 const float p1 = qd.re * h.re, p2 = qd.im * h.im;
                 eterm += p1 - p2;
                 const float sz = fabsf(p1) + fabsf(p2);
