@@ -105,6 +105,27 @@ def test_tolerance_holds(L, oracle_E, name):
     ctx.close()
 
 
+@pytest.mark.parametrize("name", ["ord4", "ord5"])
+def test_item_runs(L, oracle_E, name, monkeypatch):
+    """The same on the item runs (their estimate groups by item)."""
+    spec, c, b = case(name)
+    Eref, Gref = oracle_E[name]
+    monkeypatch.setenv("ACE_B200_KERNEL", "items")   # read at context creation
+    ctx = L.Context(spec, "fp32c")
+    monkeypatch.delenv("ACE_B200_KERNEL")
+    ctx.set_params(c)
+    ctx.set_energy_tolerance(0.0)
+    E, G = ctx.energy_forces(b.offsets, b.rr)
+    est, _ = ctx.energy_error_estimates(b.nenv)
+    assert np.all(np.abs(E - Eref) <= est)
+    tol = 1e-7
+    ctx.set_energy_tolerance(tol)
+    E, G = ctx.energy_forces(b.offsets, b.rr)
+    assert np.all(np.abs(E - Eref) <= 1.01 * tol * scale(Eref))
+    assert np.max(np.abs(G - Gref)) <= 1e-5 * np.max(np.abs(Gref))
+    ctx.close()
+
+
 def test_all_reevaluated_is_double_float(L, oracle_E):
     spec, c, b = case("ord5")
     Eref, Gref = oracle_E["ord5"]
