@@ -108,6 +108,7 @@ def test_every_entry_point_rejects_a_null_context(lib):
         "ace_radial_mlp_forward": (n, 1, n, n, n, n), "ace_radial_mlp_infer": (n, 1, n, n, n, n),
         "ace_radial_mlp_backward": (n, 1, n, n, n, n, n, n),
         "ace_energy_radial_adjoint": (n, 1, n, n, n, n, n, n, n),
+        "ace_set_energy_tolerance": (n, 1e-6), "ace_energy_error_estimates": (n, 0, n, n),
     }
     for name, args in calls.items():
         assert getattr(L, name)(*args) == INVALID, name
